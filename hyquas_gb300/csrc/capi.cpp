@@ -1,0 +1,432 @@
+// C-ABI entry points (include/hyquas_gb300.h): state objects, the plain
+// per-gate path, compiled circuits and their executor, FP64 readout.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "compiler.h"
+#include "device.h"
+#include "executor.h"
+#include "gates.h"
+
+namespace hq {
+const std::string& last_error();
+void init_explicit(int device);
+}  // namespace hq
+
+using namespace hq;
+
+#define HQ_API_BEGIN \
+    try {            \
+        clear_last_error();
+#define HQ_API_END                              \
+    return HQ_OK;                               \
+    }                                           \
+    catch (const Failure& f) {                  \
+        set_last_error(f.what());               \
+        return f.code;                          \
+    }                                           \
+    catch (const std::bad_alloc&) {             \
+        set_last_error("host allocation failed"); \
+        return HQ_ERR_NOMEM;                    \
+    }                                           \
+    catch (const std::exception& e) {           \
+        set_last_error(e.what());               \
+        return HQ_ERR_INVALID;                  \
+    }
+
+#define HQ_NONNULL(p) HQ_REQUIRE((p) != nullptr, HQ_ERR_INVALID, "%s must not be NULL", #p)
+
+extern "C" {
+
+const char* hq_last_error(void) { return hq::last_error().c_str(); }
+const char* hq_version(void) { return "hyquas_gb300 0.1 (sm_103a)"; }
+
+hq_status hq_init(int device) {
+    HQ_API_BEGIN
+    init_explicit(device);
+    HQ_API_END
+}
+
+hq_status hq_device_info(int32_t* sm_count, uint64_t* hbm_bytes, int32_t* smem_per_block) {
+    HQ_API_BEGIN
+    Context& c = ctx();
+    if (sm_count) *sm_count = c.sm_count;
+    if (hbm_bytes) *hbm_bytes = c.hbm_bytes;
+    if (smem_per_block) *smem_per_block = c.smem_optin;
+    HQ_API_END
+}
+
+hq_status hq_set_hbm_budget(uint64_t bytes) {
+    HQ_API_BEGIN
+    ctx().budget = bytes;
+    HQ_API_END
+}
+
+hq_status hq_hbm_in_use(uint64_t* bytes) {
+    HQ_API_BEGIN
+    HQ_NONNULL(bytes);
+    *bytes = ctx().in_use;
+    HQ_API_END
+}
+
+hq_status hq_host_alloc(uint64_t bytes, void** out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(out);
+    ensure_init();
+    *out = nullptr;
+    HQ_CHECK_CUDA(cudaHostAlloc(out, bytes, cudaHostAllocDefault));
+    HQ_API_END
+}
+
+hq_status hq_host_free(void* p) {
+    HQ_API_BEGIN
+    if (p) HQ_CHECK_CUDA(cudaFreeHost(p));
+    HQ_API_END
+}
+
+hq_status hq_gate_make(int32_t type, int32_t target, int32_t control, int32_t control2,
+                       const double* params, hq_gate* out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(out);
+    *out = make_gate(type, target, control, control2, params);
+    HQ_API_END
+}
+
+// ---- states ---------------------------------------------------------------------
+
+hq_status hq_state_create(int32_t n, hq_state* out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(out);
+    *out = nullptr;
+    *out = state_create(n);
+    HQ_API_END
+}
+
+hq_status hq_state_destroy(hq_state s) {
+    HQ_API_BEGIN
+    state_destroy(s);
+    HQ_API_END
+}
+
+hq_status hq_state_init_zero(hq_state s) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    launch_init_zero(s->d, s->n, ctx().stream);
+    for (int q = 0; q < s->n; q++) s->pos[q] = q;
+    HQ_CHECK_CUDA(cudaStreamSynchronize(ctx().stream));
+    HQ_API_END
+}
+
+hq_status hq_state_load(hq_state s, const float* host) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_NONNULL(host);
+    HQ_CHECK_CUDA(cudaMemcpyAsync(s->d, host, s->bytes, cudaMemcpyHostToDevice, ctx().stream));
+    for (int q = 0; q < s->n; q++) s->pos[q] = q;
+    HQ_CHECK_CUDA(cudaStreamSynchronize(ctx().stream));
+    HQ_API_END
+}
+
+hq_status hq_state_store(hq_state s, float* host) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_NONNULL(host);
+    state_canonicalize(s);
+    HQ_CHECK_CUDA(cudaMemcpyAsync(host, s->d, s->bytes, cudaMemcpyDeviceToHost, ctx().stream));
+    HQ_CHECK_CUDA(cudaStreamSynchronize(ctx().stream));
+    HQ_API_END
+}
+
+hq_status hq_state_amps(hq_state s, const uint64_t* idx, int64_t count, float* out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_REQUIRE(count >= 0, HQ_ERR_INVALID, "negative count");
+    if (count == 0) return HQ_OK;
+    HQ_NONNULL(idx);
+    HQ_NONNULL(out);
+    state_gather(s, idx, count, out);
+    HQ_API_END
+}
+
+hq_status hq_state_layout(hq_state s, int32_t* pos) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_NONNULL(pos);
+    for (int q = 0; q < s->n; q++) pos[q] = s->pos[q];
+    HQ_API_END
+}
+
+hq_status hq_state_num_qubits(hq_state s, int32_t* n) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_NONNULL(n);
+    *n = s->n;
+    HQ_API_END
+}
+
+hq_status hq_state_device_ptr(hq_state s, void** p) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_NONNULL(p);
+    *p = s->d;
+    HQ_API_END
+}
+
+hq_status hq_state_marginals(hq_state s, double* p1) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_NONNULL(p1);
+    double h[1 + 64];
+    state_marginals(s, h);
+    for (int q = 0; q < s->n; q++) p1[q] = h[1 + s->pos[q]];
+    HQ_API_END
+}
+
+hq_status hq_state_norm(hq_state s, double* norm) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_NONNULL(norm);
+    double h[1 + 64];
+    state_marginals(s, h);
+    *norm = h[0];
+    HQ_API_END
+}
+
+hq_status hq_state_prob_zero(hq_state s, int32_t q, double* p0) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_NONNULL(p0);
+    HQ_REQUIRE(q >= 0 && q < s->n, HQ_ERR_INVALID, "qubit %d out of range", q);
+    double h[1 + 64];
+    state_marginals(s, h);
+    *p0 = h[0] - h[1 + s->pos[q]];
+    HQ_API_END
+}
+
+hq_status hq_state_remap(hq_state s, const int32_t* new_pos) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_NONNULL(new_pos);
+    std::vector<int> np(new_pos, new_pos + s->n);
+    state_remap(s, np);
+    HQ_API_END
+}
+
+// ---- plain path ------------------------------------------------------------------
+
+hq_status hq_apply_gates(hq_state s, const hq_gate* gates, int32_t num_gates) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_REQUIRE(num_gates >= 0, HQ_ERR_INVALID, "negative gate count");
+    if (num_gates == 0) return HQ_OK;
+    HQ_NONNULL(gates);
+    std::vector<hq_gate> v(gates, gates + num_gates);
+    apply_plain(s, v);
+    HQ_CHECK_CUDA(cudaStreamSynchronize(ctx().stream));
+    HQ_API_END
+}
+
+hq_status hq_synchronize(void) {
+    HQ_API_BEGIN
+    HQ_CHECK_CUDA(cudaStreamSynchronize(ctx().stream));
+    check_device_error();
+    HQ_API_END
+}
+
+// ---- circuits --------------------------------------------------------------------
+
+hq_status hq_compile_options_default(hq_compile_options* opt) {
+    HQ_API_BEGIN
+    HQ_NONNULL(opt);
+    std::memset(opt, 0, sizeof(*opt));
+    opt->backend = HQ_BACKEND_OSHM;
+    opt->mm_precision = HQ_MM_BF16X3;
+    HQ_API_END
+}
+
+hq_status hq_circuit_create(int32_t n, hq_circuit* out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(out);
+    HQ_REQUIRE(n >= 1 && n <= 36, HQ_ERR_INVALID, "num_qubits %d out of range [1,36]", n);
+    auto c = new hq_circuit_s();
+    c->n = n;
+    *out = c;
+    HQ_API_END
+}
+
+hq_status hq_circuit_destroy(hq_circuit c) {
+    HQ_API_BEGIN
+    if (c) {
+        circuit_release(c);
+        delete c;
+    }
+    HQ_API_END
+}
+
+hq_status hq_circuit_add_gates(hq_circuit c, const hq_gate* gates, int32_t num_gates) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_REQUIRE(num_gates >= 0, HQ_ERR_INVALID, "negative gate count");
+    for (int i = 0; i < num_gates; i++) {
+        validate_gate(gates[i], c->n);
+        c->gates.push_back(gates[i]);
+    }
+    c->compiled = false;
+    HQ_API_END
+}
+
+hq_status hq_circuit_num_gates(hq_circuit c, int32_t* num_gates) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_NONNULL(num_gates);
+    *num_gates = (int32_t)c->gates.size();
+    HQ_API_END
+}
+
+hq_status hq_circuit_compile(hq_circuit c, const hq_compile_options* opt) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    hq_compile_options o;
+    if (opt)
+        o = *opt;
+    else
+        hq_compile_options_default(&o);
+    circuit_compile(c, o);
+    HQ_API_END
+}
+
+hq_status hq_circuit_schedule(hq_circuit c, int32_t* num_groups, int32_t* backend,
+                              int32_t* gates_per_group, int32_t* width, uint64_t* related) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
+    const auto& gs = c->part.groups;
+    if (num_groups) *num_groups = (int32_t)gs.size();
+    for (size_t i = 0; i < gs.size(); i++) {
+        if (backend) backend[i] = gs[i].backend;
+        if (gates_per_group) gates_per_group[i] = (int32_t)gs[i].gates.size();
+        if (width) width[i] = gs[i].width;
+        if (related) related[i] = gs[i].related;
+    }
+    HQ_API_END
+}
+
+hq_status hq_circuit_group_gates(hq_circuit c, int32_t g, int32_t* gate_idx, int32_t cap,
+                                 int32_t* count) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
+    HQ_REQUIRE(g >= 0 && g < (int)c->part.groups.size(), HQ_ERR_INVALID, "group %d out of range", g);
+    const auto& v = c->part.groups[g].gates;
+    if (count) *count = (int32_t)v.size();
+    if (gate_idx) {
+        HQ_REQUIRE(cap >= (int)v.size(), HQ_ERR_INVALID, "gate_idx capacity %d < %zu", cap, v.size());
+        for (size_t i = 0; i < v.size(); i++) gate_idx[i] = c->orig_index[v[i]];
+    }
+    HQ_API_END
+}
+
+hq_status hq_plan_groups(int32_t n, const hq_gate* gates, int32_t num_gates,
+                         const hq_compile_options* opt, int32_t* num_groups, int32_t* backend,
+                         int32_t* gates_per_group, int32_t* width, uint64_t* related,
+                         int32_t* phases, int32_t* gate_order) {
+    HQ_API_BEGIN
+    HQ_REQUIRE(n >= 6 && n <= 36, HQ_ERR_INVALID, "num_qubits %d out of range [6,36]", n);
+    HQ_REQUIRE(num_gates >= 0 && (num_gates == 0 || gates), HQ_ERR_INVALID, "bad gate list");
+    hq_compile_options o;
+    if (opt)
+        o = *opt;
+    else
+        hq_compile_options_default(&o);
+    std::vector<hq_gate> v(gates, gates + num_gates);
+    for (auto& g : v) validate_gate(g, n);
+    std::vector<int> perm, orig;
+    std::vector<hq_gate> folded = fold_swaps(v, n, perm);
+    for (int i = 0; i < num_gates; i++)
+        if (v[i].type != G_SWAP) orig.push_back(i);
+    CompileConfig cfg = config_from_options(o, n);
+    std::vector<int> id(n);
+    for (int q = 0; q < n; q++) id[q] = q;
+    Partition part = partition(n, folded, id, cfg);
+    if (num_groups) *num_groups = (int32_t)part.groups.size();
+    size_t k = 0;
+    for (size_t i = 0; i < part.groups.size(); i++) {
+        const GroupPlan& gp = part.groups[i];
+        if (backend) backend[i] = gp.backend;
+        if (gates_per_group) gates_per_group[i] = (int32_t)gp.gates.size();
+        if (width) width[i] = gp.width;
+        if (related) related[i] = gp.related;
+        if (phases) {
+            phases[i] = 0;
+            if (gp.backend == HQ_BACKEND_OSHM && !cfg.reference) {
+                std::vector<hq_gate> pg;
+                for (int x : gp.gates) pg.push_back(folded[x]);
+                phases[i] = (int32_t)plan_oshm(n, pg, oshm_tile_mask(gp, n)).phases.size();
+            }
+        }
+        if (gate_order)
+            for (int x : gp.gates) gate_order[k++] = orig[x];
+    }
+    HQ_API_END
+}
+
+hq_status hq_circuit_program_bytes(hq_circuit c, uint64_t* bytes) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_NONNULL(bytes);
+    HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
+    *bytes = c->phases_bytes + c->ops_bytes + c->umats_bytes + c->mm_scratch_bytes;
+    HQ_API_END
+}
+
+hq_status hq_circuit_run(hq_circuit c, hq_state s, double* elapsed_us) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_NONNULL(s);
+    const double us = circuit_run(c, s, true);
+    if (elapsed_us) *elapsed_us = us;
+    HQ_API_END
+}
+
+hq_status hq_circuit_profile(hq_circuit c, hq_state s, double* group_us) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_NONNULL(s);
+    HQ_NONNULL(group_us);
+    circuit_profile(c, s, group_us);
+    HQ_API_END
+}
+
+hq_status hq_circuit_enqueue(hq_circuit c, hq_state s) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_NONNULL(s);
+    circuit_run(c, s, false);
+    HQ_API_END
+}
+
+hq_status hq_circuit_capture_graph(hq_circuit c, hq_state s) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_NONNULL(s);
+    circuit_capture(c, s);
+    HQ_API_END
+}
+
+hq_status hq_apply_oshm_group(hq_state s, const hq_gate* gates, int32_t num_gates,
+                              uint64_t tile_mask) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_REQUIRE(num_gates >= 0 && (num_gates == 0 || gates), HQ_ERR_INVALID, "bad gate list");
+    std::vector<hq_gate> v(gates, gates + num_gates);
+    apply_oshm_group(s, v, tile_mask);
+    HQ_API_END
+}
+
+}  // extern "C"

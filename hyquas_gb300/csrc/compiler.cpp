@@ -1,0 +1,550 @@
+#include "compiler.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace hq {
+
+namespace {
+
+// Fixed-capacity bitset over a gate window (<= 2048 gates).
+struct WinSet {
+    std::vector<uint64_t> w;
+    explicit WinSet(int nbits = 0) : w((nbits + 63) / 64, 0) {}
+    void set(int i) { w[i >> 6] |= uint64_t(1) << (i & 63); }
+    bool test(int i) const { return (w[i >> 6] >> (i & 63)) & 1; }
+    int count() const {
+        int c = 0;
+        for (uint64_t x : w) c += __builtin_popcountll(x);
+        return c;
+    }
+    bool any() const {
+        for (uint64_t x : w)
+            if (x) return true;
+        return false;
+    }
+    WinSet& operator|=(const WinSet& o) {
+        for (size_t i = 0; i < w.size(); i++) w[i] |= o.w[i];
+        return *this;
+    }
+    void andnot(const WinSet& o) {
+        for (size_t i = 0; i < w.size(); i++) w[i] &= ~o.w[i];
+    }
+};
+
+struct GroupingInput {
+    int n;
+    const std::vector<hq_gate>* gates;
+    std::vector<char> diag;   // per gate: counts as diagonal for grouping
+    bool ref_semantics;       // reproduce the reference exactly (CCX control2 ignored)
+};
+
+// GateGroup::newRelated, src/schedule.cpp:35-50
+uint64_t new_related(uint64_t rel, const hq_gate& g, bool diag, uint64_t local_qubits,
+                     bool enable_global) {
+    if (enable_global) {
+        if (!diag) rel |= uint64_t(1) << g.target;
+    } else {
+        if (!diag || ((local_qubits >> g.target) & 1)) rel |= uint64_t(1) << g.target;
+        if (g.control >= 0 && ((local_qubits >> g.control) & 1)) rel |= uint64_t(1) << g.control;
+        if (g.control2 >= 0 && ((local_qubits >> g.control2) & 1)) rel |= uint64_t(1) << g.control2;
+    }
+    return rel;
+}
+
+// OneLayerCompiler::getGroupOpt, src/compiler.cpp:322-452.  Returns indices
+// (into the gate list) of the selected gates in window order.
+std::vector<int> get_group_opt(const GroupingInput& in, const std::vector<int>& remain,
+                               int max_gates, std::vector<char>& full, std::vector<uint64_t>& related,
+                               bool enable_global, int local_size, uint64_t local_qubits) {
+    const int n = in.n;
+    const auto& gates = *in.gates;
+    const int gate_num = std::min<int>(max_gates, (int)remain.size());
+    std::vector<WinSet> cur(n, WinSet(gate_num));
+    WinSet selected(gate_num);
+
+    // phase 1: per-qubit dependency chains while the related set fits
+    for (int id = 0; id < gate_num; id++) {
+        if (id % 100 == 0) {
+            bool live = false;
+            for (int i = 0; i < n; i++)
+                if (!full[i]) live = true;
+            if (!live) break;
+        }
+        const hq_gate& g = gates[remain[id]];
+        const bool dg = in.diag[remain[id]];
+        if (g.control >= 0) {
+            const int c = g.control, t = g.target;
+            const int c2 = in.ref_semantics ? -1 : g.control2;
+            if (!full[c] && !full[t] && (c2 < 0 || !full[c2])) {
+                uint64_t nr = related[c] | related[t] | (c2 >= 0 ? related[c2] : 0);
+                nr = new_related(nr, g, dg, local_qubits, enable_global);
+                if (__builtin_popcountll(nr) <= local_size) {
+                    WinSet nc = cur[c];
+                    nc |= cur[t];
+                    if (c2 >= 0) nc |= cur[c2];
+                    nc.set(id);
+                    cur[c] = nc;
+                    cur[t] = nc;
+                    related[c] = related[t] = nr;
+                    if (c2 >= 0) {
+                        cur[c2] = nc;
+                        related[c2] = nr;
+                    }
+                    continue;
+                }
+            }
+            full[c] = full[t] = 1;
+            if (c2 >= 0) full[c2] = 1;
+        } else {
+            if (!full[g.target]) {
+                cur[g.target].set(id);
+                related[g.target] = new_related(related[g.target], g, dg, local_qubits, enable_global);
+            }
+        }
+    }
+
+    // phase 2: greedy union of the largest chains that still fit
+    std::vector<char> blocked(n, 0);
+    uint64_t selected_related = 0;
+    while (true) {
+        int mx = 0, id = -1;
+        for (int i = 0; i < n; i++) {
+            const int count_i = cur[i].count();
+            if (!blocked[i] && count_i > mx) {
+                if (__builtin_popcountll(selected_related | related[i]) <= local_size) {
+                    mx = count_i;
+                    id = i;
+                } else {
+                    blocked[i] = 1;
+                }
+            }
+        }
+        if (mx == 0) break;
+        selected |= cur[id];
+        selected_related |= related[id];
+        blocked[id] = 1;
+        for (int i = 0; i < n; i++) {
+            if (!blocked[i] && cur[i].any()) {
+                if ((related[i] | selected_related) == selected_related) {
+                    selected |= cur[i];
+                    blocked[i] = 1;
+                } else {
+                    cur[i].andnot(cur[id]);
+                }
+            }
+        }
+    }
+
+    if (enable_global) {
+        // phase 3: absorb diagonal gates on qubits not blocked by a skipped gate
+        std::fill(blocked.begin(), blocked.end(), 0);
+        int cnt = 0;
+        for (int id = 0; id < gate_num; id++) {
+            cnt++;
+            if (cnt % 100 == 0) {
+                bool live = false;
+                for (int i = 0; i < n; i++)
+                    if (!blocked[i]) live = true;
+                if (!live) break;
+            }
+            if (selected.test(id)) continue;
+            const hq_gate& g = gates[remain[id]];
+            const int c2 = in.ref_semantics ? -1 : g.control2;
+            if (in.diag[remain[id]]) {
+                if (g.control >= 0) {
+                    if (!blocked[g.control] && !blocked[g.target] && (c2 < 0 || !blocked[c2])) {
+                        selected.set(id);
+                    } else {
+                        blocked[g.control] = blocked[g.target] = 1;
+                        if (c2 >= 0) blocked[c2] = 1;
+                    }
+                } else if (!blocked[g.target]) {
+                    selected.set(id);
+                }
+            } else {
+                if (g.control >= 0) blocked[g.control] = 1;
+                if (c2 >= 0) blocked[c2] = 1;
+                blocked[g.target] = 1;
+            }
+        }
+    }
+    std::vector<int> ret;
+    for (int id = 0; id < gate_num; id++)
+        if (selected.test(id)) ret.push_back(remain[id]);
+    return ret;
+}
+
+void remove_selected(std::vector<int>& remain, const std::vector<int>& sel) {
+    std::vector<int> out;
+    out.reserve(remain.size());
+    size_t j = 0;
+    for (int x : remain) {
+        while (j < sel.size() && sel[j] < x) j++;
+        if (j < sel.size() && sel[j] == x) continue;
+        out.push_back(x);
+    }
+    remain.swap(out);
+}
+
+// GateGroup::initBlasState, src/schedule.cpp:339-382: bring the group's
+// qubits to the lowest physical positions (layout only).
+void blas_layout(std::vector<int>& pos, std::vector<int>& layout, uint64_t related, int n) {
+    const int nm = __builtin_popcountll(related);
+    std::vector<int> to_global, to_local;
+    for (int i = 0; i < nm; i++)
+        if (!((related >> layout[i]) & 1)) to_global.push_back(layout[i]);
+    for (int i = nm; i < n; i++)
+        if ((related >> layout[i]) & 1) to_local.push_back(layout[i]);
+    for (size_t i = 0; i < to_global.size() && i < to_local.size(); i++) {
+        const int x = to_global[i], y = to_local[i];
+        std::swap(pos[x], pos[y]);
+        layout[pos[x]] = x;
+        layout[pos[y]] = y;
+    }
+}
+
+}  // namespace
+
+uint64_t pad_tile(uint64_t mask, int k, int n) {
+    for (int b = 0; b < n && __builtin_popcountll(mask) < k; b++) mask |= uint64_t(1) << b;
+    return mask;
+}
+
+Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
+                    const CompileConfig& cfg) {
+    Partition out;
+    GroupingInput in;
+    in.n = n;
+    in.gates = &gates;
+    in.ref_semantics = cfg.reference;
+    in.diag.resize(gates.size());
+    for (size_t i = 0; i < gates.size(); i++)
+        in.diag[i] = cfg.reference ? ref_is_diagonal(gates[i].type) : matrix_is_diagonal(gates[i]);
+
+    std::vector<int> pos = pos0, layout(n);
+    for (int q = 0; q < n; q++) layout[pos[q]] = q;
+    std::vector<int> remain(gates.size());
+    for (size_t i = 0; i < gates.size(); i++) remain[i] = (int)i;
+    const uint64_t all = n >= 64 ? ~uint64_t(0) : ((uint64_t(1) << n) - 1);
+    const int tile = cfg.reference ? 10 : std::min(cfg.tile, n);
+    const int coalesce = cfg.reference ? 3 : std::max(1, std::min(cfg.coalesce, tile));
+    const int mat = cfg.reference ? 6 : std::min(cfg.mm_qubits, n);
+
+    auto oshm_candidate = [&](uint64_t& rel_out) {
+        std::vector<char> full(n, 0);
+        uint64_t seed = 0;
+        for (int j = 0; j < coalesce && j < n; j++) seed |= uint64_t(1) << layout[j];
+        std::vector<uint64_t> related(n, seed);
+        std::vector<int> idx = get_group_opt(in, remain, 512, full, related, true, tile, all);
+        uint64_t rel = 0;
+        for (int x : idx) rel = new_related(rel, gates[x], in.diag[x], all, true);
+        rel_out = rel | seed;
+        return idx;
+    };
+    auto mm_candidate = [&](int m, uint64_t& rel_out) {
+        std::vector<char> full(n, 0);
+        std::vector<uint64_t> related(n, 0);
+        std::vector<int> idx = get_group_opt(in, remain, 512, full, related, false, m, all);
+        uint64_t rel = 0;
+        for (int x : idx) rel = new_related(rel, gates[x], in.diag[x], all, false);
+        rel_out = rel;
+        return idx;
+    };
+
+    int guard = 0;
+    while (!remain.empty()) {
+        HQ_REQUIRE(++guard < 1000000, HQ_ERR_INVALID, "partition did not converge");
+        GroupPlan gp;
+        gp.pos = pos;
+        uint64_t rel = 0;
+        std::vector<int> idx;
+        int backend = cfg.backend == HQ_BACKEND_TRANSMM ? HQ_BACKEND_TRANSMM : HQ_BACKEND_OSHM;
+        if (cfg.backend == HQ_BACKEND_HYBRID && !cfg.reference) {
+            // per-group choice by predicted time per gate (src/compiler.cpp:248-280)
+            uint64_t r_o = 0;
+            std::vector<int> io = oshm_candidate(r_o);
+            double best = 1e30;
+            if (!io.empty()) {
+                std::vector<hq_gate> gs;
+                for (int x : io) gs.push_back(gates[x]);
+                best = cost_oshm(n, 0, gs, tile) / io.size();
+            }
+            idx = io;
+            rel = r_o;
+            backend = HQ_BACKEND_OSHM;
+            for (int m = 4; m <= std::min(mat, 8); m++) {
+                uint64_t r_m = 0;
+                std::vector<int> im = mm_candidate(m, r_m);
+                if (im.empty()) continue;
+                const double eff = cost_transmm(n, std::max(m, __builtin_popcountll(r_m)),
+                                                cfg.mm_precision) / im.size();
+                if (eff < best) {
+                    best = eff;
+                    idx = im;
+                    rel = r_m;
+                    backend = HQ_BACKEND_TRANSMM;
+                }
+            }
+        } else if (backend == HQ_BACKEND_OSHM) {
+            idx = oshm_candidate(rel);
+        } else {
+            idx = mm_candidate(mat, rel);
+        }
+        if (idx.empty()) {  // cannot happen for valid widths; keep progress anyway
+            idx.push_back(remain.front());
+            rel = gate_qubits(gates[remain.front()]);
+        }
+        gp.backend = backend;
+        gp.gates = idx;
+        gp.related = rel;
+        if (backend == HQ_BACKEND_OSHM) {
+            gp.width = tile;
+        } else {
+            gp.width = std::max(__builtin_popcountll(rel), cfg.reference ? 4 : 1);
+            if (cfg.reference) blas_layout(pos, layout, rel, n);
+        }
+        gp.pos_after = pos;
+        remove_selected(remain, idx);
+        out.groups.push_back(std::move(gp));
+    }
+    out.final_pos = pos;
+    return out;
+}
+
+// ---- OShareMem lowering ---------------------------------------------------------
+
+namespace {
+
+// smem slot class of a local tile bit: which of slot bits 0..3 it moves
+// (see the swizzle in k_oshm.cu)
+int slot_class(int b) { return b <= 3 ? b : 1 + (b - 4) % 3; }
+
+}  // namespace
+
+OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_mask) {
+    OshmProgram prog;
+    const int k = __builtin_popcountll(tile_mask);
+    HQ_REQUIRE(k >= 6 && k <= OSHM_MAX_K && k <= n, HQ_ERR_INVALID, "oshm: tile width %d", k);
+    HQ_REQUIRE(tile_mask & 1, HQ_ERR_INVALID, "oshm: tile must contain physical qubit 0");
+    const int r = oshm_reg_bits(k);
+    prog.n = n;
+    prog.k = k;
+    prog.r = r;
+    prog.tile_mask = tile_mask;
+    int loc[64];
+    int phys_of[OSHM_MAX_K];
+    for (int b = 0, j = 0; b < 64; b++) {
+        loc[b] = -1;
+        if ((tile_mask >> b) & 1) {
+            loc[b] = j;
+            phys_of[j] = b;
+            j++;
+        }
+    }
+    std::vector<char> diag(gates.size());
+    for (size_t i = 0; i < gates.size(); i++) {
+        diag[i] = matrix_is_diagonal(gates[i]);
+        HQ_REQUIRE(diag[i] || loc[gates[i].target] >= 0, HQ_ERR_INVALID,
+                   "oshm: non-diagonal gate on qubit %d outside the tile", gates[i].target);
+    }
+
+    std::vector<char> done(gates.size(), 0);
+    size_t ndone = 0;
+    while (ndone < gates.size()) {
+        // choose this phase's register bits greedily in gate order
+        uint32_t rset = 0;  // local bits
+        uint64_t blocked = 0;
+        std::vector<int> members;
+        for (size_t i = 0; i < gates.size(); i++) {
+            if (done[i]) continue;
+            const hq_gate& g = gates[i];
+            const uint64_t q = gate_qubits(g);
+            if (q & blocked) {
+                blocked |= q;
+                continue;
+            }
+            if (!diag[i]) {
+                const uint32_t tl = 1u << loc[g.target];
+                if (!(rset & tl)) {
+                    if (__builtin_popcount(rset) >= r) {
+                        blocked |= q;
+                        continue;
+                    }
+                    rset |= tl;
+                }
+            }
+            members.push_back((int)i);
+        }
+        HQ_REQUIRE(!members.empty(), HQ_ERR_INVALID, "oshm: planner made no progress");
+        // pad the register set to r bits: local bit 0 first (16-byte accesses)
+        for (int b = 0; b < k && __builtin_popcount(rset) < r; b++) rset |= 1u << b;
+
+        OshmPhase ph;
+        std::memset(&ph, 0, sizeof(ph));
+        int r_local[OSHM_MAX_R];
+        int nr = 0;
+        ph.pair0 = (rset & 1u) ? 1 : 0;
+        if (ph.pair0) r_local[nr++] = 0;
+        for (int b = 1; b < k; b++)
+            if ((rset >> b) & 1) r_local[nr++] = b;
+        for (int j = 0; j < r; j++) ph.r_local[j] = (uint8_t)r_local[j];
+        int reg_of_local[OSHM_MAX_K];
+        for (int b = 0; b < k; b++) reg_of_local[b] = -1;
+        for (int j = 0; j < r; j++) reg_of_local[r_local[j]] = j;
+
+        // thread-index bits: lane bits chosen for conflict-free smem accesses
+        std::vector<int> gfree;
+        for (int b = 0; b < k; b++)
+            if (!((rset >> b) & 1)) gfree.push_back(b);
+        std::vector<int> order;
+        auto take_class = [&](int cls) {
+            for (size_t i = 0; i < gfree.size(); i++)
+                if (slot_class(gfree[i]) == cls) {
+                    order.push_back(gfree[i]);
+                    gfree.erase(gfree.begin() + i);
+                    return;
+                }
+        };
+        if (!ph.pair0) take_class(0);
+        take_class(1);
+        take_class(2);
+        take_class(3);
+        for (int b : gfree) order.push_back(b);
+        for (size_t j = 0; j < order.size(); j++) {
+            ph.g_local[j] = (uint8_t)order[j];
+            ph.g_phys[j] = (uint8_t)phys_of[order[j]];
+        }
+
+        ph.op_begin = (uint32_t)prog.ops.size();
+        for (int i : members) {
+            const hq_gate& g = gates[i];
+            OshmOp o;
+            std::memset(&o, 0, sizeof(o));
+            for (int q = 0; q < 8; q++) o.m[q] = (float)g.mat[q];
+            auto add_ctrl = [&](int c) {
+                if (c < 0) return;
+                const int lc = loc[c];
+                if (lc >= 0 && reg_of_local[lc] >= 0)
+                    o.creg |= 1u << reg_of_local[lc];
+                else
+                    o.cout |= uint64_t(1) << c;
+            };
+            add_ctrl(g.control);
+            add_ctrl(g.control2);
+            const int lt = loc[g.target];
+            const int rt = lt >= 0 ? reg_of_local[lt] : -1;
+            if (diag[i]) {
+                o.d0_is_one = (g.mat[0] == 1.0 && g.mat[1] == 0.0) ? 1 : 0;
+                if (g.mat[6] == 1.0 && g.mat[7] == 0.0 && o.d0_is_one) continue;  // identity
+                if (rt >= 0) {
+                    o.kind = OP_DREG;
+                    o.tbit = (uint8_t)rt;
+                } else {
+                    o.kind = OP_DOUT;
+                    o.tout = uint64_t(1) << g.target;
+                }
+            } else {
+                o.tbit = (uint8_t)rt;
+                const bool real = g.mat[1] == 0 && g.mat[3] == 0 && g.mat[5] == 0 && g.mat[7] == 0;
+                if (is_x_like(g))
+                    o.kind = OP_X;
+                else if (real)
+                    o.kind = OP_REAL;
+                else
+                    o.kind = OP_U;
+            }
+            prog.ops.push_back(o);
+        }
+        ph.op_end = (uint32_t)prog.ops.size();
+        prog.phases.push_back(ph);
+        for (int i : members) done[i] = 1;
+        ndone += members.size();
+    }
+    return prog;
+}
+
+OshmLaunch make_oshm_launch(const OshmProgram& prog, void* state, const OshmPhase* d_phases,
+                            const OshmOp* d_ops, int* d_err) {
+    OshmLaunch p;
+    std::memset(&p, 0, sizeof(p));
+    const int n = prog.n, k = prog.k, r = prog.r;
+    p.state = state;
+    p.phases = d_phases;
+    p.ops = d_ops;
+    p.err = d_err;
+    p.n = n;
+    p.k = k;
+    p.nphases = (int)prog.phases.size();
+    p.ntiles = uint64_t(1) << (n - k);
+    for (int b = 0, j = 0; b < n; b++)
+        if ((prog.tile_mask >> b) & 1) p.tile_phys[j++] = (uint8_t)b;
+    // runs of block bits: tile index bit i -> physical bit
+    int src = 0, nruns = 0;
+    for (int b = 0; b < n;) {
+        if ((prog.tile_mask >> b) & 1) {
+            b++;
+            continue;
+        }
+        int len = 0;
+        while (b + len < n && !((prog.tile_mask >> (b + len)) & 1)) len++;
+        HQ_REQUIRE(nruns < 32, HQ_ERR_INVALID, "oshm: too many block-bit runs");
+        p.run_src[nruns] = (uint8_t)src;
+        p.run_dst[nruns] = (uint8_t)b;
+        p.run_len[nruns] = (uint8_t)len;
+        nruns++;
+        src += len;
+        b += len;
+    }
+    p.nruns = nruns;
+    // pieces: thread t handles piece t + m*T (local index 2*(t + m*T))
+    const int T = oshm_threads(k, r);
+    const int ppt = (1 << (k - 1)) / T;
+    HQ_REQUIRE(ppt <= 32, HQ_ERR_INVALID, "oshm: piece table");
+    for (int m = 0; m < ppt; m++) {
+        const uint32_t local = uint32_t(2 * m * T);
+        uint64_t off = 0;
+        for (int j = 0; j < k; j++)
+            if ((local >> j) & 1) off |= uint64_t(1) << p.tile_phys[j];
+        p.piece_off[m] = off;
+        p.piece_slot[m] = oshm_swizzle(local);
+    }
+    return p;
+}
+
+// ---- GB300 cost model --------------------------------------------------------
+// Seconds per pass, refitted constants (see costmodel section of the design
+// notes): a pass moves 16 * 2^n bytes; OShareMem compute is ~4 instructions
+// per amplitude per non-diagonal gate on 152 SMs x 128 lanes; TransMM runs
+// 3 BF16 products on the tensor pipe.
+static const double kHbmBytesPerSec = 5.6e12;      // sustained pass bandwidth
+static const double kSimtInstrPerSec = 3.3e13;     // issued thread-instructions
+static const double kTensorFlopsPerSec = 1.5e15;   // BF16 dense, sustained
+static const double kLaunchSec = 4e-6;
+
+double cost_oshm(int n, int nphases, const std::vector<hq_gate>& gates, int k) {
+    (void)k;
+    const double amps = double(uint64_t(1) << n);
+    double instr = 6.0;  // staging
+    for (const auto& g : gates) instr += matrix_is_diagonal(g) ? 1.0 : (is_x_like(g) ? 1.5 : 4.5);
+    instr += 4.0 * (nphases > 0 ? nphases : 1 + (double)gates.size() / 12.0);
+    const double t_mem = 16.0 * amps / kHbmBytesPerSec;
+    const double t_cmp = instr * amps / kSimtInstrPerSec;
+    return std::max(t_mem, t_cmp) + kLaunchSec;
+}
+
+double cost_transmm(int n, int m, int precision) {
+    const double amps = double(uint64_t(1) << n);
+    const double t_mem = 16.0 * amps / kHbmBytesPerSec;
+    const double flops = 8.0 * amps * double(uint64_t(1) << m);
+    double t_cmp;
+    if (precision == HQ_MM_FP32)
+        t_cmp = flops / 6.0e13;
+    else if (precision == HQ_MM_TF32)
+        t_cmp = flops / (kTensorFlopsPerSec / 2);
+    else
+        t_cmp = 3.0 * flops / kTensorFlopsPerSec;
+    return std::max(t_mem, t_cmp) + kLaunchSec;
+}
+
+}  // namespace hq

@@ -1,0 +1,408 @@
+#include "executor.h"
+
+#include <algorithm>
+#include <cstring>
+
+#include "common.h"
+#include "transmm.h"
+
+namespace hq {
+
+// ---- states ---------------------------------------------------------------------
+
+static size_t marg_scratch_doubles(int n) {
+    const uint64_t nquads = (uint64_t(1) << n) / 2;
+    const uint64_t nb1 = (nquads + 2047) / 2048;
+    const uint64_t nb2 = (nb1 + 4095) / 4096;
+    return size_t(nb1 * 13 + nb2 * 25);
+}
+
+hq_state_s* state_create(int n) {
+    HQ_REQUIRE(n >= 1 && n <= 36, HQ_ERR_INVALID, "num_qubits %d out of range [1,36]", n);
+    ensure_init();
+    auto s = new hq_state_s();
+    s->n = n;
+    s->bytes = sizeof(float) * 2 * (size_t(1) << n);
+    s->pos.resize(n);
+    for (int q = 0; q < n; q++) s->pos[q] = q;
+    try {
+        s->d = dev_alloc(s->bytes);
+        s->scratch_doubles = marg_scratch_doubles(n);
+        s->d_scratch = (double*)dev_alloc(sizeof(double) * s->scratch_doubles);
+    } catch (...) {
+        if (s->d) dev_free(s->d, s->bytes);
+        delete s;
+        throw;
+    }
+    return s;
+}
+
+void state_destroy(hq_state_s* s) {
+    if (!s) return;
+    if (s->d) dev_free(s->d, s->bytes);
+    if (s->d_scratch) dev_free(s->d_scratch, sizeof(double) * s->scratch_doubles);
+    delete s;
+}
+
+void state_remap(hq_state_s* s, const std::vector<int>& np) {
+    const int n = s->n;
+    HQ_REQUIRE((int)np.size() == n, HQ_ERR_INVALID, "remap: layout size");
+    std::vector<char> seen(n, 0);
+    for (int q = 0; q < n; q++) {
+        HQ_REQUIRE(np[q] >= 0 && np[q] < n && !seen[np[q]], HQ_ERR_INVALID,
+                   "remap: not a permutation");
+        seen[np[q]] = 1;
+    }
+    cudaStream_t st = ctx().stream;
+    for (int q = 0; q < n; q++) {
+        if (s->pos[q] == np[q]) continue;
+        int q2 = -1;
+        for (int x = 0; x < n; x++)
+            if (s->pos[x] == np[q]) q2 = x;
+        launch_bit_swap(s->d, n, s->pos[q], np[q], st);
+        s->pos[q2] = s->pos[q];
+        s->pos[q] = np[q];
+    }
+}
+
+void state_canonicalize(hq_state_s* s) {
+    std::vector<int> id(s->n);
+    for (int q = 0; q < s->n; q++) id[q] = q;
+    state_remap(s, id);
+}
+
+void state_gather(hq_state_s* s, const uint64_t* idx, int64_t count, float* out) {
+    const int n = s->n;
+    std::vector<uint64_t> phys(count);
+    for (int64_t i = 0; i < count; i++) {
+        HQ_REQUIRE(n >= 64 || idx[i] < (uint64_t(1) << n), HQ_ERR_INVALID,
+                   "amplitude index %llu out of range", (unsigned long long)idx[i]);
+        uint64_t p = 0;
+        for (int q = 0; q < n; q++)
+            if ((idx[i] >> q) & 1) p |= uint64_t(1) << s->pos[q];
+        phys[i] = p;
+    }
+    cudaStream_t st = ctx().stream;
+    const size_t ib = sizeof(uint64_t) * count, ob = sizeof(float) * 2 * count;
+    char* buf = (char*)dev_alloc(ib + ob);
+    try {
+        HQ_CHECK_CUDA(cudaMemcpyAsync(buf, phys.data(), ib, cudaMemcpyHostToDevice, st));
+        launch_gather(s->d, (const uint64_t*)buf, count, buf + ib, st);
+        HQ_CHECK_CUDA(cudaMemcpyAsync(out, buf + ib, ob, cudaMemcpyDeviceToHost, st));
+        HQ_CHECK_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+        dev_free(buf, ib + ob);
+        throw;
+    }
+    dev_free(buf, ib + ob);
+}
+
+void state_marginals(hq_state_s* s, double* h) {
+    launch_marginals(s->d, s->n, s->d_scratch, s->scratch_doubles, h, ctx().stream);
+}
+
+// ---- plain path ------------------------------------------------------------------
+
+static PlainGate lower_plain(const hq_gate& g, const std::vector<int>& pos) {
+    PlainGate p;
+    std::memset(&p, 0, sizeof(p));
+    p.target = pos[g.target];
+    int ins[3], ni = 0;
+    ins[ni++] = p.target;
+    if (g.control >= 0) {
+        ins[ni++] = pos[g.control];
+        p.setmask |= uint64_t(1) << pos[g.control];
+    }
+    if (g.control2 >= 0) {
+        ins[ni++] = pos[g.control2];
+        p.setmask |= uint64_t(1) << pos[g.control2];
+    }
+    std::sort(ins, ins + ni);
+    p.ninsert = ni;
+    for (int i = 0; i < ni; i++) p.insert[i] = ins[i];
+    for (int i = 0; i < 8; i++) p.m[i] = (float)g.mat[i];
+    if (is_x_like(g))
+        p.kind = PK_SWAP;
+    else if (matrix_is_diagonal(g))
+        p.kind = (g.mat[0] == 1.0 && g.mat[1] == 0.0) ? PK_DIAG_HI : PK_DIAG;
+    else
+        p.kind = PK_GENERAL;
+    return p;
+}
+
+void apply_plain(hq_state_s* s, const std::vector<hq_gate>& gates) {
+    cudaStream_t st = ctx().stream;
+    for (const hq_gate& g : gates) {
+        validate_gate(g, s->n);
+        if (g.type == G_SWAP) {
+            // exchange the two qubits' physical positions in the layout (no data pass)
+            std::swap(s->pos[g.target], s->pos[g.control]);
+            continue;
+        }
+        launch_plain_gate(s->d, s->n, lower_plain(g, s->pos), st);
+    }
+}
+
+void apply_oshm_group(hq_state_s* s, const std::vector<hq_gate>& gates, uint64_t tile_logical) {
+    const int n = s->n;
+    std::vector<hq_gate> phys;
+    for (const hq_gate& g0 : gates) {
+        validate_gate(g0, n);
+        HQ_REQUIRE(g0.type != G_SWAP, HQ_ERR_INVALID, "oshm group: SWAP not allowed");
+        hq_gate g = g0;
+        g.target = s->pos[g0.target];
+        if (g0.control >= 0) g.control = s->pos[g0.control];
+        if (g0.control2 >= 0) g.control2 = s->pos[g0.control2];
+        phys.push_back(g);
+    }
+    uint64_t tile = 0;
+    for (int q = 0; q < n; q++)
+        if ((tile_logical >> q) & 1) tile |= uint64_t(1) << s->pos[q];
+    OshmProgram prog = plan_oshm(n, phys, tile);
+    const size_t pb = sizeof(OshmPhase) * std::max<size_t>(1, prog.phases.size());
+    const size_t ob = sizeof(OshmOp) * std::max<size_t>(1, prog.ops.size());
+    char* buf = (char*)dev_alloc(pb + ob);
+    cudaStream_t st = ctx().stream;
+    try {
+        HQ_CHECK_CUDA(cudaMemcpyAsync(buf, prog.phases.data(), sizeof(OshmPhase) * prog.phases.size(),
+                                      cudaMemcpyHostToDevice, st));
+        HQ_CHECK_CUDA(cudaMemcpyAsync(buf + pb, prog.ops.data(), sizeof(OshmOp) * prog.ops.size(),
+                                      cudaMemcpyHostToDevice, st));
+        OshmLaunch p = make_oshm_launch(prog, s->d, (const OshmPhase*)buf, (const OshmOp*)(buf + pb),
+                                        ctx().d_error);
+        launch_oshm(p, st);
+        HQ_CHECK_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+        dev_free(buf, pb + ob);
+        throw;
+    }
+    dev_free(buf, pb + ob);
+    check_device_error();
+}
+
+// ---- circuits ---------------------------------------------------------------------
+
+void circuit_release(hq_circuit_s* c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    c->graph_state = nullptr;
+    if (c->d_phases) dev_free(c->d_phases, c->phases_bytes);
+    if (c->d_ops) dev_free(c->d_ops, c->ops_bytes);
+    if (c->d_umats) dev_free(c->d_umats, c->umats_bytes);
+    if (c->d_mm_scratch) dev_free(c->d_mm_scratch, c->mm_scratch_bytes);
+    c->d_phases = nullptr;
+    c->d_ops = nullptr;
+    c->d_umats = nullptr;
+    c->d_mm_scratch = nullptr;
+    c->phases_bytes = c->ops_bytes = c->umats_bytes = c->mm_scratch_bytes = 0;
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    c->ev0 = c->ev1 = nullptr;
+    c->dgroups.clear();
+    c->compiled = false;
+}
+
+CompileConfig config_from_options(const hq_compile_options& o, int n) {
+    CompileConfig cfg;
+    cfg.backend = o.backend;
+    cfg.reference = o.reference_grouping != 0;
+    cfg.tile = o.tile_qubits > 0 ? o.tile_qubits : 13;
+    cfg.coalesce = o.coalesce > 0 ? o.coalesce : 3;
+    cfg.mm_qubits = o.mm_qubits > 0 ? o.mm_qubits : 6;
+    cfg.mm_precision = o.mm_precision;
+    HQ_REQUIRE(o.backend == HQ_BACKEND_PLAIN || o.backend == HQ_BACKEND_OSHM ||
+                   o.backend == HQ_BACKEND_TRANSMM || o.backend == HQ_BACKEND_HYBRID,
+               HQ_ERR_INVALID, "unknown backend %d", o.backend);
+    HQ_REQUIRE(cfg.tile >= 6 && cfg.tile <= OSHM_MAX_K, HQ_ERR_INVALID,
+               "tile_qubits %d out of range [6,%d]", cfg.tile, OSHM_MAX_K);
+    HQ_REQUIRE(cfg.mm_qubits >= 1 && cfg.mm_qubits <= 8, HQ_ERR_INVALID,
+               "mm_qubits %d out of range [1,8]", cfg.mm_qubits);
+    HQ_REQUIRE(o.mm_precision >= HQ_MM_BF16X3 && o.mm_precision <= HQ_MM_FP32, HQ_ERR_INVALID,
+               "unknown TransMM precision %d", o.mm_precision);
+    HQ_REQUIRE(cfg.coalesce >= 1, HQ_ERR_INVALID, "coalesce must be >= 1");
+    cfg.tile = std::min(cfg.tile, n);
+    return cfg;
+}
+
+uint64_t oshm_tile_mask(const GroupPlan& gp, int n) {
+    // the group's related qubits (they include the coalesced low qubits, so
+    // physical qubit 0) padded with the lowest free qubits to the tile width
+    uint64_t tile = pad_tile(gp.related | 1, gp.width, n);
+    HQ_REQUIRE(__builtin_popcountll(tile) == gp.width, HQ_ERR_INVALID,
+               "oshm: related set wider than the tile (%d > %d)", __builtin_popcountll(tile),
+               gp.width);
+    return tile;
+}
+
+void circuit_compile(hq_circuit_s* c, const hq_compile_options& o) {
+    circuit_release(c);
+    ensure_init();
+    const int n = c->n;
+    c->opt = o;
+    // SWAP folding: drop swaps, relabel the gates after them
+    std::vector<int> perm;
+    c->folded = fold_swaps(c->gates, n, perm);
+    c->swap_perm = perm;
+    c->orig_index.clear();
+    for (size_t i = 0; i < c->gates.size(); i++)
+        if (c->gates[i].type != G_SWAP) c->orig_index.push_back((int)i);
+
+    CompileConfig cfg = config_from_options(o, n);
+    if (o.backend == HQ_BACKEND_PLAIN || n < 6) {
+        // one launch per gate; small registers always take this path
+        c->part = Partition();
+        c->part.final_pos.resize(n);
+        for (int q = 0; q < n; q++) c->part.final_pos[q] = q;
+        c->compiled = true;
+        return;
+    }
+    std::vector<int> id(n);
+    for (int q = 0; q < n; q++) id[q] = q;
+    c->part = partition(n, c->folded, id, cfg);
+
+    std::vector<OshmPhase> phases;
+    std::vector<OshmOp> ops;
+    std::vector<double> umats;
+    for (const GroupPlan& gp : c->part.groups) {
+        DeviceGroup dg;
+        dg.backend = gp.backend;
+        // execution keeps the identity layout: a group's gates act on their
+        // qubits in place (TransMM gathers its rows, no transpose pass)
+        for (int x : gp.gates) dg.phys_gates.push_back(c->folded[x]);
+        if (gp.backend == HQ_BACKEND_OSHM) {
+            dg.prog = plan_oshm(n, dg.phys_gates, oshm_tile_mask(gp, n));
+            dg.phase_off = phases.size();
+            dg.op_off = ops.size();
+            for (auto ph : dg.prog.phases) {
+                ph.op_begin += (uint32_t)dg.op_off;
+                ph.op_end += (uint32_t)dg.op_off;
+                phases.push_back(ph);
+            }
+            ops.insert(ops.end(), dg.prog.ops.begin(), dg.prog.ops.end());
+        } else {
+            transmm_prepare(n, gp, dg, cfg, umats);
+        }
+        c->dgroups.push_back(std::move(dg));
+    }
+    cudaStream_t st = ctx().stream;
+    if (!phases.empty()) {
+        c->phases_bytes = sizeof(OshmPhase) * phases.size();
+        c->d_phases = (OshmPhase*)dev_alloc(c->phases_bytes);
+        HQ_CHECK_CUDA(cudaMemcpyAsync(c->d_phases, phases.data(), c->phases_bytes,
+                                      cudaMemcpyHostToDevice, st));
+    }
+    if (!ops.empty()) {
+        c->ops_bytes = sizeof(OshmOp) * ops.size();
+        c->d_ops = (OshmOp*)dev_alloc(c->ops_bytes);
+        HQ_CHECK_CUDA(cudaMemcpyAsync(c->d_ops, ops.data(), c->ops_bytes, cudaMemcpyHostToDevice, st));
+    }
+    if (!umats.empty()) {
+        c->umats_bytes = sizeof(double) * umats.size();
+        c->d_umats = (double*)dev_alloc(c->umats_bytes);
+        HQ_CHECK_CUDA(cudaMemcpyAsync(c->d_umats, umats.data(), c->umats_bytes,
+                                      cudaMemcpyHostToDevice, st));
+    }
+    transmm_finalize(c);
+    HQ_CHECK_CUDA(cudaStreamSynchronize(st));
+    c->compiled = true;
+}
+
+void circuit_launch_groups(hq_circuit_s* c, void* state, cudaStream_t st) {
+    for (const DeviceGroup& dg : c->dgroups) {
+        if (dg.backend == HQ_BACKEND_OSHM) {
+            OshmLaunch p = make_oshm_launch(dg.prog, state, c->d_phases + dg.phase_off,
+                                            c->d_ops, ctx().d_error);
+            launch_oshm(p, st);
+        } else {
+            transmm_launch(c, dg, state, st);
+        }
+    }
+}
+
+double circuit_run(hq_circuit_s* c, hq_state_s* s, bool sync) {
+    HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
+    HQ_REQUIRE(s->n == c->n, HQ_ERR_INVALID, "state has %d qubits, circuit %d", s->n, c->n);
+    cudaStream_t st = ctx().stream;
+    state_canonicalize(s);
+    if (!c->ev0) {
+        HQ_CHECK_CUDA(cudaEventCreate(&c->ev0));
+        HQ_CHECK_CUDA(cudaEventCreate(&c->ev1));
+    }
+    HQ_CHECK_CUDA(cudaEventRecord(c->ev0, st));
+    if (c->opt.backend == HQ_BACKEND_PLAIN || c->n < 6) {
+        apply_plain(s, c->folded);
+    } else if (c->graph && c->graph_state == s) {
+        HQ_CHECK_CUDA(cudaGraphLaunch(c->graph, st));
+    } else {
+        circuit_launch_groups(c, s->d, st);
+    }
+    HQ_CHECK_CUDA(cudaEventRecord(c->ev1, st));
+    for (int q = 0; q < c->n; q++) s->pos[q] = c->swap_perm[q];
+    if (!sync) return 0.0;
+    HQ_CHECK_CUDA(cudaEventSynchronize(c->ev1));
+    check_device_error();
+    float ms = 0.f;
+    HQ_CHECK_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    return double(ms) * 1000.0;
+}
+
+void circuit_profile(hq_circuit_s* c, hq_state_s* s, double* group_us) {
+    HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
+    HQ_REQUIRE(s->n == c->n, HQ_ERR_INVALID, "state/circuit size mismatch");
+    HQ_REQUIRE(c->opt.backend != HQ_BACKEND_PLAIN && c->n >= 6, HQ_ERR_STATE,
+               "plain-path circuits have no groups to profile");
+    cudaStream_t st = ctx().stream;
+    state_canonicalize(s);
+    const size_t ng = c->dgroups.size();
+    std::vector<cudaEvent_t> ev(ng + 1);
+    for (auto& e : ev) HQ_CHECK_CUDA(cudaEventCreate(&e));
+    HQ_CHECK_CUDA(cudaEventRecord(ev[0], st));
+    for (size_t g = 0; g < ng; g++) {
+        const DeviceGroup& dg = c->dgroups[g];
+        if (dg.backend == HQ_BACKEND_OSHM) {
+            OshmLaunch p = make_oshm_launch(dg.prog, s->d, c->d_phases + dg.phase_off, c->d_ops,
+                                            ctx().d_error);
+            launch_oshm(p, st);
+        } else {
+            transmm_launch(c, dg, s->d, st);
+        }
+        HQ_CHECK_CUDA(cudaEventRecord(ev[g + 1], st));
+    }
+    HQ_CHECK_CUDA(cudaEventSynchronize(ev[ng]));
+    for (size_t g = 0; g < ng; g++) {
+        float ms = 0.f;
+        HQ_CHECK_CUDA(cudaEventElapsedTime(&ms, ev[g], ev[g + 1]));
+        group_us[g] = double(ms) * 1000.0;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    for (int q = 0; q < c->n; q++) s->pos[q] = c->swap_perm[q];
+    check_device_error();
+}
+
+void circuit_capture(hq_circuit_s* c, hq_state_s* s) {
+    HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
+    HQ_REQUIRE(s->n == c->n, HQ_ERR_INVALID, "state/circuit size mismatch");
+    if (c->opt.backend == HQ_BACKEND_PLAIN || c->n < 6) return;  // nothing to capture
+    cudaStream_t st = ctx().stream;
+    HQ_CHECK_CUDA(cudaStreamSynchronize(st));
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    HQ_CHECK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+        circuit_launch_groups(c, s->d, st);
+    } catch (...) {
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    HQ_CHECK_CUDA(cudaStreamEndCapture(st, &g));
+    cudaError_t e = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    HQ_REQUIRE(e == cudaSuccess, HQ_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    c->graph_state = s;
+}
+
+}  // namespace hq

@@ -1,0 +1,237 @@
+/* hyquas_gb300 -- GB300-native single-GPU state-vector simulator, C ABI.
+ *
+ * This is the drop-in boundary for the single-GPU path of thu-pacman/HyQuas.
+ * Every entry point names the reference interface it replaces (path:line in
+ * the reference tree).  The header-only C++ facade in hyquas_gb300/circuit.hpp
+ * re-creates the reference's Circuit/Gate API (src/circuit.h:20-46,
+ * src/gate.h:11-66) on top of these functions; ctypes bindings in
+ * hyquas_gb300/__init__.py do the same for Python.
+ *
+ * Conventions
+ *   - Plain C types only: pointers, sizes, int32/int64/uint64, float, double.
+ *   - Every function returns an hq_status (0 = success).  hq_last_error()
+ *     returns a thread-local message for the last failure.  The reference
+ *     exits the process on any error (src/utils.h:106-144); here errors are
+ *     returned and the library stays usable.
+ *   - State vectors are complex64, interleaved (re, im), 2^n amplitudes, the
+ *     reference's qComplex layout for the FP32 build (src/utils.h:24-31).
+ *     Amplitude index bit q is qubit q.
+ *   - After a compiled run the amplitudes may sit in a permuted qubit layout
+ *     (the reference keeps its final State, src/circuit.cpp:95-113).  All
+ *     readout functions take LOGICAL indices and apply the layout.
+ *   - Objects are not thread-safe; use one object per host thread.
+ */
+#ifndef HYQUAS_GB300_H
+#define HYQUAS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t hq_status;
+#define HQ_OK 0
+#define HQ_ERR_INVALID (-1)     /* bad argument: qubit index, size, null pointer */
+#define HQ_ERR_CUDA (-2)        /* a CUDA runtime/driver call failed */
+#define HQ_ERR_NOMEM (-3)       /* device allocation failed or over the HBM budget */
+#define HQ_ERR_STATE (-4)       /* object in the wrong state (e.g. run before compile) */
+#define HQ_ERR_TIMEOUT (-5)     /* a bounded device-side wait expired (error flag set) */
+#define HQ_ERR_UNSUPPORTED (-6) /* feature not available on this device/configuration */
+#define HQ_ERR_BUSY (-7)        /* serving queue full / slot not ready */
+
+/* Gate type ordinals follow the reference GateType (src/gate.h:7-9). */
+enum hq_gate_type {
+    HQ_CCX = 0, HQ_CNOT = 1, HQ_CY = 2, HQ_CZ = 3, HQ_CRX = 4, HQ_CRY = 5, HQ_CU1 = 6,
+    HQ_CRZ = 7, HQ_U1 = 8, HQ_U2 = 9, HQ_U3 = 10, HQ_H = 11, HQ_X = 12, HQ_Y = 13,
+    HQ_Z = 14, HQ_S = 15, HQ_SDG = 16, HQ_T = 17, HQ_TDG = 18, HQ_RX = 19, HQ_RY = 20,
+    HQ_RZ = 21, HQ_ID = 23,
+    /* Extension (no reference counterpart): exchange of qubits `target` and
+     * `control`.  The compiler folds it into the qubit layout (no data pass). */
+    HQ_SWAP = 28
+};
+
+/* One gate: the fields of the reference Gate (src/gate.h:11-20) without the
+ * name/id.  mat = row-major 2x2 complex in double: re00 im00 re01 im01 re10
+ * im10 re11 im11.  control/control2 = -1 when absent. */
+typedef struct hq_gate {
+    int32_t type;
+    int32_t target;
+    int32_t control;
+    int32_t control2;
+    double mat[8];
+} hq_gate;
+
+typedef struct hq_state_s* hq_state;
+typedef struct hq_circuit_s* hq_circuit;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Select the device and create the library's stream.  Replaces
+ * MyGlobalVars::init (src/utils.cpp:17-60) for one GPU; idempotent. */
+hq_status hq_init(int device);
+/* Thread-local message for the last failing call ("" when none). */
+const char* hq_last_error(void);
+/* Library version string. */
+const char* hq_version(void);
+/* Device facts: SM count, HBM bytes, max shared memory per block. */
+hq_status hq_device_info(int32_t* sm_count, uint64_t* hbm_bytes, int32_t* smem_per_block);
+/* Set the HBM budget (bytes) that state allocation is admitted against;
+ * 0 = no budget.  No reference counterpart (the reference has no admission). */
+hq_status hq_set_hbm_budget(uint64_t bytes);
+hq_status hq_hbm_in_use(uint64_t* bytes);
+
+/* Page-locked host buffers for fast state transfers (cudaHostAlloc). */
+hq_status hq_host_alloc(uint64_t bytes, void** out);
+hq_status hq_host_free(void* p);
+
+/* ---- gates (src/gate.cpp:9-342, the Gate::* factories) ---------------- */
+
+/* Fill `out` with the gate of `type` on the given qubits; params = the
+ * factory's angle arguments in order (theta/phi/lambda/angle), may be NULL
+ * for gates without angles.  Argument order of the reference factories is
+ * control-then-target; here qubits are passed by role. */
+hq_status hq_gate_make(int32_t type, int32_t target, int32_t control, int32_t control2,
+                       const double* params, hq_gate* out);
+
+/* ---- state vector (src/kernelSimple.cu:9-37, 518-529) ------------------ */
+
+/* Allocate a 2^n complex64 state (no initialisation).  kernelInit's cudaMalloc,
+ * src/kernelSimple.cu:9-37. */
+hq_status hq_state_create(int32_t num_qubits, hq_state* out);
+/* kernelDestroy, src/kernelSimple.cu:527-529. */
+hq_status hq_state_destroy(hq_state s);
+/* |0..0>: kernelInit's memset + amp[0]=1, src/kernelSimple.cu:14-31. */
+hq_status hq_state_init_zero(hq_state s);
+/* Upload 2^n interleaved complex64 amplitudes in logical order; resets the
+ * layout to identity.  No reference counterpart (random initial states). */
+hq_status hq_state_load(hq_state s, const float* host_amps);
+/* Download all 2^n amplitudes in LOGICAL order (undoing the layout on the
+ * device first).  kernelDeviceToHost + Circuit::ampAt, src/kernelSimple.cu:523-525,
+ * src/circuit.cpp:54-64, 115-118. */
+hq_status hq_state_store(hq_state s, float* host_amps);
+/* Download the amplitudes at `count` logical indices.  Circuit::ampAtGPU /
+ * kernelGetAmp, src/circuit.cpp:120-142, src/kernelSimple.cu:518-522. */
+hq_status hq_state_amps(hq_state s, const uint64_t* logical_idx, int64_t count, float* out);
+/* Current logical->physical qubit map (State::pos, src/schedule.h:15-34). */
+hq_status hq_state_layout(hq_state s, int32_t* pos);
+hq_status hq_state_num_qubits(hq_state s, int32_t* n);
+/* Device pointer of the amplitudes (physical order); for zero-copy users. */
+hq_status hq_state_device_ptr(hq_state s, void** dev_ptr);
+
+/* P(qubit q = 0) with an FP64 reduction: kernelMeasure, src/kernelSimple.cu:497-516. */
+hq_status hq_state_prob_zero(hq_state s, int32_t logical_qubit, double* p0);
+/* sum |a|^2 (FP64 reduction). */
+hq_status hq_state_norm(hq_state s, double* norm);
+/* P(qubit q = 1) for every logical qubit, one FP64 pass. */
+hq_status hq_state_marginals(hq_state s, double* p1);
+/* ---- plain path (BACKEND=serial): one launch per gate ------------------- */
+
+/* Apply gates one kernel launch each, in order: kernelExecSimple,
+ * src/kernelSimple.cu:335-446.  Logical qubits, current layout honoured. */
+hq_status hq_apply_gates(hq_state s, const hq_gate* gates, int32_t num_gates);
+
+/* ---- circuits: compile + run (src/circuit.cpp:16-71, 156-210) ------------ */
+
+/* Backends, after the reference's -DBACKEND (CMakeLists.txt:18-35). */
+enum hq_backend {
+    HQ_BACKEND_PLAIN = 0,   /* serial: one launch per gate */
+    HQ_BACKEND_OSHM = 1,    /* group: OShareMem gate groups only */
+    HQ_BACKEND_TRANSMM = 3, /* blas: TransMM groups only */
+    HQ_BACKEND_HYBRID = 4   /* mix: per-group cost-model choice */
+};
+/* TransMM arithmetic. */
+enum hq_mm_precision {
+    HQ_MM_BF16X3 = 0, /* split hi+lo BF16, 3 products, FP32 accumulate (tcgen05) */
+    HQ_MM_TF32 = 1,   /* one TF32 product (tcgen05) */
+    HQ_MM_FP32 = 2    /* FP32 SIMT */
+};
+
+typedef struct hq_compile_options {
+    int32_t backend;       /* hq_backend */
+    int32_t tile_qubits;   /* OShareMem tile width k (0 = autotuned) */
+    int32_t coalesce;      /* low physical qubits always in a tile (0 = default) */
+    int32_t mm_qubits;     /* TransMM group width (0 = autotuned, else 4..8) */
+    int32_t mm_precision;  /* hq_mm_precision */
+    int32_t reference_grouping; /* 1 = use the reference's widths (tile 10, coalesce 3, MAT 6) */
+} hq_compile_options;
+
+hq_status hq_compile_options_default(hq_compile_options* opt);
+
+hq_status hq_circuit_create(int32_t num_qubits, hq_circuit* out);
+hq_status hq_circuit_destroy(hq_circuit c);
+/* Circuit::addGate, src/circuit.h:28-30. */
+hq_status hq_circuit_add_gates(hq_circuit c, const hq_gate* gates, int32_t num_gates);
+hq_status hq_circuit_num_gates(hq_circuit c, int32_t* num_gates);
+/* Circuit::compile, src/circuit.cpp:177-210 (Compiler::run, src/compiler.cpp:70-165). */
+hq_status hq_circuit_compile(hq_circuit c, const hq_compile_options* opt);
+/* Number of gate groups and, per group: backend (HQ_BACKEND_OSHM /
+ * HQ_BACKEND_TRANSMM), gate count, tile/group width and related-qubit mask.
+ * Arrays may be NULL; they must hold num_groups entries otherwise. */
+hq_status hq_circuit_schedule(hq_circuit c, int32_t* num_groups, int32_t* backend,
+                              int32_t* gates_per_group, int32_t* width, uint64_t* related);
+/* Gate indices (into the added list) of group g, in execution order. */
+hq_status hq_circuit_group_gates(hq_circuit c, int32_t g, int32_t* gate_idx, int32_t cap,
+                                 int32_t* count);
+/* Host-only planning (no device needed): partition `num_gates` gates as
+ * hq_circuit_compile would and report, per group, its backend, gate count,
+ * width, related-qubit mask and (OShareMem) number of register phases;
+ * gate_order receives the gate indices group after group (num_gates
+ * entries).  Arrays need room for num_gates groups.  The CPU half of
+ * Circuit::compile (src/circuit.cpp:156-175, Compiler::run
+ * src/compiler.cpp:70-165). */
+hq_status hq_plan_groups(int32_t num_qubits, const hq_gate* gates, int32_t num_gates,
+                         const hq_compile_options* opt, int32_t* num_groups, int32_t* backend,
+                         int32_t* gates_per_group, int32_t* width, uint64_t* related,
+                         int32_t* phases, int32_t* gate_order);
+/* Bytes of device-resident program (gate-group lowering, fused unitaries)
+ * that compile uploaded for this circuit. */
+hq_status hq_circuit_program_bytes(hq_circuit c, uint64_t* bytes);
+/* Run the compiled schedule on state s (stream-ordered, then synchronised).
+ * Circuit::run, src/circuit.cpp:16-71; elapsed_us = device time of the run
+ * (the reference's "Time Cost"). */
+hq_status hq_circuit_run(hq_circuit c, hq_state s, double* elapsed_us);
+/* Run the compiled schedule on s with a CUDA event pair around every group;
+ * group_us[g] = device time of group g (num_groups entries).  The reference's
+ * MEASURE_STAGE per-group timing, src/executor.cpp:406-458. */
+hq_status hq_circuit_profile(hq_circuit c, hq_state s, double* group_us);
+/* Enqueue the compiled schedule on the library stream without synchronising. */
+hq_status hq_circuit_enqueue(hq_circuit c, hq_state s);
+/* Capture the compiled schedule for state s into a CUDA graph (replayed by
+ * later hq_circuit_run / hq_circuit_enqueue calls on the same state). */
+hq_status hq_circuit_capture_graph(hq_circuit c, hq_state s);
+hq_status hq_synchronize(void);
+
+/* ---- single group entry points (the reference kernel ABI, src/kernel.h) -- */
+
+/* One OShareMem pass over the state applying `num_gates` gates (logical
+ * qubits) whose non-diagonal targets lie in `tile_mask` (logical qubit mask,
+ * popcount = tile width).  Replaces copyGatesToSymbol + launchExecutor,
+ * src/kernel.h:20-25, src/kernelOpt.cu:499-506. */
+hq_status hq_apply_oshm_group(hq_state s, const hq_gate* gates, int32_t num_gates,
+                              uint64_t tile_mask);
+/* One TransMM pass: fuse the gates (all on the qubits of `group_mask`) into a
+ * 2^m x 2^m unitary (FP64 composition on the GPU) and apply it with the given
+ * arithmetic.  Replaces GateGroup::initMatrix + cuttExecute + cublasGEMM,
+ * src/executor.cpp:533-551. */
+hq_status hq_apply_transmm_group(hq_state s, const hq_gate* gates, int32_t num_gates,
+                                 uint64_t group_mask, int32_t precision);
+/* Apply a caller-given 2^m x 2^m unitary (column-major complex128, m =
+ * popcount(group_mask), logical qubit j of the mask = local bit j). */
+hq_status hq_apply_unitary(hq_state s, const double* unitary, uint64_t group_mask,
+                           int32_t precision);
+/* Fused FP64 unitary of gates on the qubits of group_mask, composed on the
+ * GPU, copied to host (column-major complex128).  GateGroup::initCPUMatrix,
+ * src/schedule.cpp:578-702. */
+hq_status hq_group_unitary(const hq_gate* gates, int32_t num_gates, uint64_t group_mask,
+                           double* unitary_out);
+/* Permute qubits in HBM: after the call logical qubit q sits at physical bit
+ * new_pos[q].  The single-GPU form of the reference's transpose + all-to-all
+ * (src/executor.cpp:59-179). */
+hq_status hq_state_remap(hq_state s, const int32_t* new_pos);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

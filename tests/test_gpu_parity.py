@@ -1,0 +1,261 @@
+"""GPU parity: every CUDA path against the FP64 oracle (and the reference's own
+fused-unitary outputs in tests/golden).  Tolerance for the complex64 state:
+max |d amp| <= 1e-5 and 1 - fidelity <= 1e-6 (the spec error bar)."""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from hyquas_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+TOL = 1e-5
+FID = 1e-6
+ALL_TYPES = list(range(22))
+NPARAMS = {W.CRX: 1, W.CRY: 1, W.CU1: 1, W.CRZ: 1, W.U1: 1, W.U2: 2, W.U3: 3, W.RX: 1, W.RY: 1, W.RZ: 1}
+
+
+def check(O, ref, got, tol=TOL):
+    c = O.compare(ref, got)
+    assert c["max_abs_err"] <= tol, c
+    assert c["one_minus_fidelity"] <= FID, c
+    return c
+
+
+def random_circuit(seed, n, count, types=ALL_TYPES, qubits=None):
+    rng = W.SplitMix64(seed)
+    qubits = list(range(n)) if qubits is None else qubits
+    desc = []
+    for _ in range(count):
+        t = types[rng.below(len(types))]
+        qs = rng.shuffle(qubits)[:3]
+        params = tuple(rng.uniform() * W.TWO_PI for _ in range(NPARAMS.get(t, 0)))
+        if t == W.CCX:
+            desc.append((t, qs[2], qs[0], qs[1], ()))
+        elif t <= W.CRZ:
+            desc.append((t, qs[1], qs[0], -1, params))
+        else:
+            desc.append((t, qs[0], -1, -1, params))
+    return desc
+
+
+def test_plain_config1_u3_cnot_n20(hq, oracle):
+    n = 20
+    desc = W.plain_u3_cnot(1, n, 10)
+    s = hq.State(n)
+    s.apply_gates(W.to_gates(desc))
+    check(oracle, oracle.run_f64(n, desc), s.store())
+    assert abs(s.norm() - 1.0) < 1e-5
+
+
+@pytest.mark.parametrize("t", ALL_TYPES)
+def test_plain_every_gate_type(hq, oracle, t):
+    n = 9
+    desc = random_circuit(100 + t, n, 12, types=[t])
+    psi = W.random_state(7, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    s.apply_gates(W.to_gates(desc))
+    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+
+
+@pytest.mark.parametrize("t", ALL_TYPES)
+def test_oshm_every_gate_type_in_and_out_of_tile(hq, oracle, t):
+    """One OShareMem pass (n=15, 13-qubit tile {0..12}): controls and diagonal
+    targets may sit outside the tile (qubits 13, 14)."""
+    n = 15
+    rng = W.SplitMix64(200 + t)
+    tile = list(range(13))
+    desc = []
+    for _ in range(40):
+        qs = rng.shuffle(range(n))
+        diag = t in (W.CZ, W.CU1, W.CRZ, W.U1, W.Z, W.S, W.SDG, W.T, W.TDG, W.RZ)
+        tq = qs[0] if diag else [q for q in qs if q in tile][0]
+        others = [q for q in qs if q != tq]
+        params = tuple(rng.uniform() * W.TWO_PI for _ in range(NPARAMS.get(t, 0)))
+        if t == W.CCX:
+            desc.append((t, tq, others[0], others[1], ()))
+        elif t <= W.CRZ:
+            desc.append((t, tq, others[0], -1, params))
+        else:
+            desc.append((t, tq, -1, -1, params))
+    psi = W.random_state(9, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    s.apply_oshm_group(W.to_gates(desc), (1 << 13) - 1)
+    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_oshm_scattered_tile(hq, oracle, seed):
+    """Tile = qubit 0 + 12 random qubits of 18; gates of every type with
+    non-diagonal targets in the tile, diagonal ones anywhere."""
+    n = 18
+    rng = W.SplitMix64(300 + seed)
+    tile = sorted([0] + rng.shuffle(range(1, n))[:12])
+    diag_types = [W.CZ, W.CU1, W.CRZ, W.U1, W.Z, W.S, W.SDG, W.T, W.TDG, W.RZ]
+    desc = random_circuit(400 + seed, n, 150, types=[t for t in ALL_TYPES if t not in diag_types],
+                          qubits=tile)
+    desc += random_circuit(500 + seed, n, 60, types=diag_types)
+    order = rng.shuffle(range(len(desc)))
+    desc = [desc[i] for i in order]
+    mask = sum(1 << q for q in tile)
+    psi = W.random_state(11 + seed, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    s.apply_oshm_group(W.to_gates(desc), mask)
+    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+
+
+@pytest.mark.parametrize("backend,tile,prec", [
+    ("oshm", 13, "bf16x3"), ("oshm", 10, "bf16x3"), ("oshm", 8, "bf16x3"),
+    ("transmm", 0, "fp32"), ("hybrid", 13, "fp32"), ("plain", 0, "fp32")])
+@pytest.mark.parametrize("n", [16, 20])
+def test_compiled_random_circuits(hq, oracle, backend, tile, prec, n):
+    desc = random_circuit(600 + n, n, 400)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile(backend=backend, tile_qubits=tile, precision=prec)
+    psi = W.random_state(13, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    c.run_on(s)
+    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+
+
+@pytest.mark.parametrize("n", [6, 7, 8])
+def test_golden_reference_outputs(hq, oracle, n):
+    """The reference's own fused-unitary result for the same circuit."""
+    z = np.load(GOLDEN / f"unitary_n{n}.npz")
+    desc = [tuple(x[:4]) + (tuple(x[4]),) for x in json.loads(str(z["desc"]))]
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile(backend="oshm", tile_qubits=n)
+    s = hq.State(n, zero=False)
+    s.load(z["psi"].astype(np.complex64))
+    c.run_on(s)
+    check(oracle, z["out_psi"], s.store())
+    c.run()
+    check(oracle, z["out_zero"], c.result)
+
+
+def test_swap_folding_and_logical_readout(hq, oracle):
+    n = 14
+    desc = random_circuit(700, n, 120)
+    desc.insert(40, (W.SWAP, 2, 11, -1, ()))
+    desc.insert(90, (W.SWAP, 0, 5, -1, ()))
+    desc.append((W.SWAP, 3, 13, -1, ()))
+    ref = oracle.run_f64(n, desc)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile(backend="oshm", tile_qubits=10)
+    c.run(copy_back=False, destroy=False)
+    assert c.state.layout() != list(range(n))
+    idx = np.array([0, 1, 5, 77, 1000, (1 << n) - 1], dtype=np.uint64)
+    got = c.state.amps(idx)
+    np.testing.assert_allclose(got, ref[idx.astype(np.int64)], atol=TOL)
+    for q in (0, 2, 11):
+        p0 = np.sum(np.abs(ref[((np.arange(1 << n) >> q) & 1) == 0]) ** 2)
+        assert abs(c.state.prob_zero(q) - p0) < 1e-6
+    m = c.state.marginals()
+    for q in range(n):
+        p1 = np.sum(np.abs(ref[((np.arange(1 << n) >> q) & 1) == 1]) ** 2)
+        assert abs(m[q] - p1) < 1e-6
+    check(oracle, ref, c.state.store())
+    assert c.state.layout() == list(range(n))
+
+
+def test_marginals_large_state(hq, oracle):
+    n = 26  # two reduction levels
+    psi = W.random_state(21, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    p = np.abs(psi.astype(np.complex128)) ** 2
+    assert abs(s.norm() - p.sum()) < 1e-9
+    m = s.marginals()
+    idx = np.arange(1 << n)
+    for q in (0, 1, 11, 12, 23, 24, 25):
+        assert abs(m[q] - p[((idx >> q) & 1) == 1].sum()) < 1e-9
+
+
+def test_group_unitary_fp64_matches_oracle(hq, oracle):
+    desc = random_circuit(800, 7, 90)
+    U = hq.group_unitary(W.to_gates(desc), (1 << 7) - 1)
+    np.testing.assert_allclose(U, oracle.group_unitary(list(range(7)), desc), atol=1e-12)
+
+
+@pytest.mark.parametrize("prec", ["fp32"])
+@pytest.mark.parametrize("m", [4, 5, 6, 7])
+def test_transmm_single_group(hq, oracle, prec, m):
+    n = 17
+    rng = W.SplitMix64(900 + m)
+    qubits = sorted(rng.shuffle(range(n))[:m])
+    desc = random_circuit(910 + m, n, 30 * m, qubits=qubits)
+    psi = W.random_state(17, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    s.apply_transmm_group(W.to_gates(desc), sum(1 << q for q in qubits), prec)
+    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+
+
+def inverse(desc):
+    inv = {W.T: W.TDG, W.TDG: W.T, W.S: W.SDG, W.SDG: W.S}
+    out = []
+    for (t, q, c, c2, p) in reversed(desc):
+        if t in (W.RX, W.RY, W.RZ, W.CU1, W.U1, W.CRX, W.CRY, W.CRZ):
+            out.append((t, q, c, c2, (-p[0],)))
+        else:
+            out.append((inv.get(t, t), q, c, c2, p))
+    return out
+
+
+def test_grid30_oshm_vs_plain_full_size(hq, oracle):
+    """Config 2 at full size (8 GiB): the OShareMem schedule and the plain
+    per-gate path are independent CUDA paths; they must agree, and the state
+    must stay normalised."""
+    n = 30
+    desc = W.grid_random(2, 5, 6, 20)
+    gates = W.to_gates(desc)
+    c = hq.Circuit(n)
+    c.addGates(gates)
+    c.compile(backend="oshm")
+    s1 = hq.State(n)
+    c.run_on(s1)
+    assert abs(s1.norm() - 1.0) < 1e-4
+    s2 = hq.State(n)
+    s2.apply_gates(gates)
+    idx = np.concatenate([np.arange(4096), np.array(W.SplitMix64(5).shuffle(range(1 << 20))[:4096]) << 10])
+    idx = idx.astype(np.uint64)
+    a, b = s1.amps(idx), s2.amps(idx)
+    assert np.max(np.abs(a - b)) < TOL
+    m1, m2 = s1.marginals(), s2.marginals()
+    assert np.max(np.abs(m1 - m2)) < 1e-5
+    # round trip: circuit followed by its inverse returns |0..0>
+    ci = hq.Circuit(n)
+    ci.addGates(W.to_gates(inverse(desc)))
+    ci.compile(backend="oshm")
+    ci.run_on(s1)
+    amp0 = s1.amps(np.array([0], dtype=np.uint64))[0]
+    assert abs(abs(amp0) ** 2 - 1.0) < 1e-4
+
+
+def test_qft28_analytic_amplitudes(hq, oracle):
+    """QFT |x> has amplitudes exp(2 pi i x k / N) / sqrt(N) (with the final
+    swaps); checked on sampled k at 28 qubits, a size-independent property."""
+    n = 28
+    x = 0x5A3C1F7
+    desc = [(W.X, q, -1, -1, ()) for q in range(n) if (x >> q) & 1] + W.qft(n)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile(backend="oshm")
+    s = hq.State(n)
+    c.run_on(s)
+    ks = np.array([0, 1, 2, 12345, (1 << n) - 1] + W.SplitMix64(9).shuffle(range(1 << 20))[:64],
+                  dtype=np.uint64)
+    got = s.amps(ks)
+    N = float(1 << n)
+    ref = np.exp(2j * np.pi * ((x * ks.astype(np.float64)) % N) / N) / math.sqrt(N)
+    assert np.max(np.abs(got - ref)) < 1e-6
