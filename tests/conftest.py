@@ -14,8 +14,14 @@ def pytest_configure(config):
 
 
 def _build_once():
-    from hyquas_gb300 import build as B
-    B.build()
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("hq_build", ROOT / "hyquas_gb300" / "build.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build()
+    import subprocess
+    subprocess.run(["make", "-C", str(ROOT / "oracle"), "liboracle.so"], check=True,
+                   capture_output=True)
 
 
 _build_once()
