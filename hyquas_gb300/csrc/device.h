@@ -48,14 +48,14 @@ constexpr int OSHM_MAX_R = 5;      // register bits per thread (32 amplitudes)
 constexpr int OSHM_MAX_K = 13;     // tile bits
 constexpr int OSHM_MAX_G = OSHM_MAX_K;  // thread-index bits
 
-struct OshmPhase {
+struct alignas(16) OshmPhase {
     uint32_t op_begin, op_end;
     uint8_t r_local[OSHM_MAX_R];  // local tile bit of register bit j
     uint8_t g_local[OSHM_MAX_G];  // local tile bit of thread-index bit j
     uint8_t g_phys[OSHM_MAX_G];   // physical bit of thread-index bit j
     uint8_t pair0;                // local bit 0 is register bit 0 (16-byte smem accesses)
-    uint8_t pad[4];
 };
+static_assert(sizeof(OshmPhase) == 48, "OshmPhase layout");
 
 struct OshmProgramHeader {
     int32_t k;            // tile bits

@@ -159,7 +159,8 @@ void apply_oshm_group(hq_state_s* s, const std::vector<hq_gate>& gates, uint64_t
     for (int q = 0; q < n; q++)
         if ((tile_logical >> q) & 1) tile |= uint64_t(1) << s->pos[q];
     OshmProgram prog = plan_oshm(n, phys, tile);
-    const size_t pb = sizeof(OshmPhase) * std::max<size_t>(1, prog.phases.size());
+    // ops start on a 256-byte boundary: OshmOp holds 64-bit fields
+    const size_t pb = (sizeof(OshmPhase) * std::max<size_t>(1, prog.phases.size()) + 255) & ~size_t(255);
     const size_t ob = sizeof(OshmOp) * std::max<size_t>(1, prog.ops.size());
     char* buf = (char*)dev_alloc(pb + ob);
     cudaStream_t st = ctx().stream;
