@@ -7,6 +7,8 @@
 // src/kernelSimple.cu:338).  Every kernel is HBM-bound.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "common.h"
 #include "device.h"
 
@@ -189,6 +191,31 @@ unsigned grid_for(uint64_t work, int threads) {
     return (unsigned)(blocks < cap ? (blocks ? blocks : 1) : cap);
 }
 
+// Allocation-free variant: the final reduction of the level-2 rows runs on
+// the device too, so the whole reduction is stream-ordered and needs no host
+// buffer.  Row order and FP64 addition order match launch_marginals.
+__global__ void k_marg_final(const double* __restrict__ rows2, uint64_t nb2, int n,
+                             double* __restrict__ out) {
+    const int b = threadIdx.x;  // b < n: P(bit b = 1); b == n: total
+    if (b > n) return;
+    double acc = 0.0;
+    for (uint64_t r = 0; r < nb2; r++) {
+        const double* row = rows2 + r * kMargRow2;
+        if (b == n)
+            acc += row[0];
+        else if (b < 12)
+            acc += row[1 + b];
+        else if (b < 24)
+            acc += row[13 + (b - 12)];
+        else if ((r >> (b - 24)) & 1)
+            acc += row[0];
+    }
+    if (b == n)
+        out[0] = acc;
+    else
+        out[1 + b] = acc;
+}
+
 }  // namespace
 
 void launch_plain_gate(void* state, int n, const PlainGate& g, void* stream) {
@@ -262,4 +289,77 @@ void launch_bit_swap(void* state, int n, int a, int b, void* stream) {
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 
+// ---- allocation-free marginals ------------------------------------------------
+//
+// For callers that cannot call cudaMalloc: code whose device memory is owned
+// by another allocator (a framework's caching pool or an admission budget
+// that has already handed out every byte of HBM), and latency-critical
+// paths where cudaMalloc's implicit device synchronisation is not allowed.
+// They pass the state and a device output buffer; the reduction partials
+// live in the static array below, which every GPU that loads this library
+// holds until the process exits.
+
+constexpr int kNoAllocMaxQubits = 26;
+constexpr uint64_t kNoAllocRows1 = (uint64_t(1) << (kNoAllocMaxQubits - 1)) / 2048;  // 16384
+constexpr uint64_t kNoAllocRows2 = (kNoAllocRows1 + 4095) / 4096;                    // 4
+constexpr uint64_t kNoAllocDoubles = kNoAllocRows1 * kMargRow1 + kNoAllocRows2 * kMargRow2;
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];  // 1.6 MiB
+
+// Host-side address of g_noalloc_scratch on each device: the array's name in
+// host code is only a stand-in, so the address is looked up once per device,
+// with that device current, by the first call made on it.
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_dev_ptr[128];
+
+static double* noalloc_scratch_current_device() {
+    int dev = -1;
+    HQ_CHECK_CUDA(cudaGetDevice(&dev));
+    HQ_REQUIRE(dev >= 0 && dev < 128, HQ_ERR_UNSUPPORTED, "device ordinal %d", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_dev_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        HQ_REQUIRE(e == cudaSuccess, HQ_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s",
+                   cudaGetErrorString(e));
+        g_noalloc_dev_ptr[dev] = (double*)p;
+    }
+    return g_noalloc_dev_ptr[dev];
+}
+
 }  // namespace hq
+
+extern "C" hq_status hq_marginals_noalloc(const void* d_state, int32_t num_qubits, double* d_out,
+                                          void* stream) {
+    using namespace hq;
+    try {
+        clear_last_error();
+        HQ_REQUIRE(d_state != nullptr && d_out != nullptr, HQ_ERR_INVALID,
+                   "d_state and d_out must not be NULL");
+        HQ_REQUIRE(num_qubits >= 1 && num_qubits <= kNoAllocMaxQubits, HQ_ERR_INVALID,
+                   "num_qubits %d outside the allocation-free range [1,%d] (static scratch of %llu "
+                   "doubles)",
+                   num_qubits, kNoAllocMaxQubits, (unsigned long long)kNoAllocDoubles);
+        HQ_REQUIRE(((uintptr_t)d_state & 15) == 0 && ((uintptr_t)d_out & 7) == 0, HQ_ERR_INVALID,
+                   "d_state must be 16-byte and d_out 8-byte aligned");
+        double* scratch = noalloc_scratch_current_device();
+        cudaStream_t st = (cudaStream_t)stream;
+        const int n = num_qubits;
+        const uint64_t nquads = (uint64_t(1) << n) / 2;
+        const uint64_t nb1 = (nquads + 2047) / 2048;
+        const uint64_t nb2 = (nb1 + 4095) / 4096;
+        double* rows1 = scratch;                    // every row read below is written first
+        double* rows2 = scratch + nb1 * kMargRow1;  // by this call: nothing needs clearing
+        k_marg_l1<<<(unsigned)nb1, 256, 0, st>>>((const float4*)d_state, nquads, rows1);
+        k_marg_l2<<<(unsigned)nb2, 256, 0, st>>>(rows1, nb1, rows2);
+        k_marg_final<<<1, 64, 0, st>>>(rows2, nb2, n, d_out);
+        HQ_CHECK_CUDA(cudaGetLastError());
+    } catch (const Failure& f) {
+        set_last_error(f.what());
+        return f.code;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return HQ_ERR_INVALID;
+    }
+    return HQ_OK;
+}

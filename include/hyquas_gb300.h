@@ -126,6 +126,24 @@ hq_status hq_state_prob_zero(hq_state s, int32_t logical_qubit, double* p0);
 hq_status hq_state_norm(hq_state s, double* norm);
 /* P(qubit q = 1) for every logical qubit, one FP64 pass. */
 hq_status hq_state_marginals(hq_state s, double* p1);
+/* Allocation-free form of hq_state_marginals, for callers that cannot call
+ * cudaMalloc: code whose device memory belongs to another allocator (a
+ * framework's caching pool, or an HBM budget already handed out in full) and
+ * latency-critical paths that must not take cudaMalloc's implicit device
+ * synchronisation.  No counterpart in the reference.
+ *   d_state  caller's device array of 2^num_qubits complex64 amplitudes
+ *            (16-byte aligned), read in physical order;
+ *   d_out    caller's device array of num_qubits + 1 doubles, receives
+ *            [sum |a|^2, P(bit 0 = 1), ..., P(bit n-1 = 1)] (FP64);
+ *   stream   cudaStream_t to run on (NULL = default stream); nothing is
+ *            synchronised.
+ * Scratch is a static 1.6 MiB device array in the library (held by every GPU
+ * that loads it until exit), so num_qubits is limited to 26; larger sizes
+ * return HQ_ERR_INVALID.  The first call on a device looks up the array's
+ * address with that device current: make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race. */
+hq_status hq_marginals_noalloc(const void* d_state, int32_t num_qubits, double* d_out,
+                               void* stream);
 /* ---- plain path (BACKEND=serial): one launch per gate ------------------- */
 
 /* Apply gates one kernel launch each, in order: kernelExecSimple,
