@@ -193,8 +193,9 @@ def run_ours(args, dist: Dist):
     from hyquas_gb300 import workloads as W
 
     hq.init(dist.local)
-    n = N_QUBITS
-    desc = W.grid_random(2, 5, 6, 20)
+    rows, cols = args.grid
+    n = rows * cols
+    desc = W.grid_random(2, rows, cols, 20)
     gates = W.to_gates(desc)
     circ = hq.Circuit(n)
     circ.addGates(gates)
@@ -242,10 +243,10 @@ def run_ours(args, dist: Dist):
                 "launches_per_circuit": len(dom)}
 
     # e2e through the public API with host buffers
-    pinned = hq.PinnedBuffer(1 << n)
+    pinned = hq.PinnedBuffer(1 << n) if not args.no_e2e else None
     e2e_times = []
     h2d = 0
-    for i in range(args.steps):
+    for i in range(0 if args.no_e2e else args.steps):
         t0 = time.perf_counter()
         c2 = hq.Circuit(n)
         c2.addGates(gates)
@@ -256,29 +257,35 @@ def run_ours(args, dist: Dist):
         state.store(pinned.array)
         e2e_times.append(time.perf_counter() - t0)
         del c2
-    e2e_s = dist.max(sum(e2e_times))
-    e2e = {"value": dist.ws * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(8 * (1 << n))}
-    pinned.free()
+    e2e = None
+    if not args.no_e2e:
+        e2e_s = dist.max(sum(e2e_times))
+        e2e = {"value": dist.ws * args.steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(8 * (1 << n))}
+        pinned.free()
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         state.free()
         spg, k = cpu_sample(n, desc, args.cpu_budget, threads)
+        if (rows, cols) != (5, 6):
+            cpu = None
         cpu = {"value": 1.0 / (spg * len(desc)), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"first {k} of {len(desc)} gates at n=30 (complex64 OpenMP gate-by-gate "
                          f"port of the reference semantics), scaled to the full circuit"}
 
     groups_oshm = sum(1 for b in kinds if b == hq.BACKEND_OSHM)
+    workload = WORKLOAD if (rows, cols) == (5, 6) else WORKLOAD.replace(
+        "grid 5x6 (30 qubits)", f"grid {rows}x{cols} ({n} qubits)")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "backend": args.backend, "passes": len(sched),
+        "config": {"workload": workload, "backend": args.backend, "passes": len(sched),
                    "oshm_groups": groups_oshm, "transmm_groups": len(sched) - groups_oshm,
                    "reference_groups_tile10": 17, "compile_ms": compile_ms,
-                   "l2": "state (8 GiB) larger than L2; no flush",
+                   "l2": f"state ({8 << n >> 20} MiB) larger than L2; no flush",
                    "parallelism": f"replicas x{dist.ws}"},
         "roofline": roofline,
         "cpu_baseline": cpu,
@@ -300,7 +307,11 @@ def main():
     ap.add_argument("--backend", default="oshm", choices=["oshm", "hybrid", "transmm"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU sampling")
+    ap.add_argument("--grid", default="5x6", help="grid RxC of the circuit (5x6 = the 30-qubit "
+                    "benchmark; smaller grids are for profiler captures)")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
+    args.grid = tuple(int(x) for x in args.grid.lower().split("x"))
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     dist = Dist()
     try:
