@@ -1,6 +1,7 @@
 #include "compiler.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 namespace hq {
@@ -322,6 +323,28 @@ int slot_class(int b) { return b <= 3 ? b : 1 + (b - 4) % 3; }
 
 }  // namespace
 
+namespace {
+
+bool close(double a, double b) { return std::fabs(a - b) < 1e-12; }
+
+// Hadamard-like 2x2 matrices that the kernel runs as adds with a deferred
+// 1/sqrt(2): H, RY(pi/2) (sqrt(Y)), RX(pi/2) (sqrt(X)).
+int hadamard_like(const hq_gate& g) {
+    const double c = 1.0 / std::sqrt(2.0);
+    const double* m = g.mat;
+    auto is = [&](double r00, double i00, double r01, double i01, double r10, double i10, double r11,
+                  double i11) {
+        return close(m[0], r00) && close(m[1], i00) && close(m[2], r01) && close(m[3], i01) &&
+               close(m[4], r10) && close(m[5], i10) && close(m[6], r11) && close(m[7], i11);
+    };
+    if (is(c, 0, c, 0, c, 0, -c, 0)) return OP_H;
+    if (is(c, 0, -c, 0, c, 0, c, 0)) return OP_SY;
+    if (is(c, 0, 0, -c, 0, -c, c, 0)) return OP_SX;
+    return -1;
+}
+
+}  // namespace
+
 OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_mask) {
     OshmProgram prog;
     const int k = __builtin_popcountll(tile_mask);
@@ -349,11 +372,15 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
                    "oshm: non-diagonal gate on qubit %d outside the tile", gates[i].target);
     }
 
+    const double rsqrt2 = 1.0 / std::sqrt(2.0);
+    double pending_scale = 1.0;  // deferred 1/sqrt2 factors not applied yet
+    int pending_count = 0;
     std::vector<char> done(gates.size(), 0);
     size_t ndone = 0;
     while (ndone < gates.size()) {
-        // choose this phase's register bits greedily in gate order
-        uint32_t rset = 0;  // local bits
+        // register qubits of this phase: local qubit 0 always (the f32x2 lane),
+        // plus up to r-1 targets chosen greedily in gate order
+        uint32_t rset = 1u;
         uint64_t blocked = 0;
         std::vector<int> members;
         for (size_t i = 0; i < gates.size(); i++) {
@@ -377,15 +404,13 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
             members.push_back((int)i);
         }
         HQ_REQUIRE(!members.empty(), HQ_ERR_INVALID, "oshm: planner made no progress");
-        // pad the register set to r bits: local bit 0 first (16-byte accesses)
-        for (int b = 0; b < k && __builtin_popcount(rset) < r; b++) rset |= 1u << b;
+        for (int b = 1; b < k && __builtin_popcount(rset) < r; b++) rset |= 1u << b;
 
         OshmPhase ph;
         std::memset(&ph, 0, sizeof(ph));
         int r_local[OSHM_MAX_R];
         int nr = 0;
-        ph.pair0 = (rset & 1u) ? 1 : 0;
-        if (ph.pair0) r_local[nr++] = 0;
+        r_local[nr++] = 0;
         for (int b = 1; b < k; b++)
             if ((rset >> b) & 1) r_local[nr++] = b;
         for (int j = 0; j < r; j++) ph.r_local[j] = (uint8_t)r_local[j];
@@ -393,7 +418,8 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
         for (int b = 0; b < k; b++) reg_of_local[b] = -1;
         for (int j = 0; j < r; j++) reg_of_local[r_local[j]] = j;
 
-        // thread-index bits: lane bits chosen for conflict-free smem accesses
+        // thread-index bits: the first three give conflict-free 16-byte smem
+        // accesses within a quarter warp (distinct swizzle classes 1, 2, 3)
         std::vector<int> gfree;
         for (int b = 0; b < k; b++)
             if (!((rset >> b) & 1)) gfree.push_back(b);
@@ -406,7 +432,6 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
                     return;
                 }
         };
-        if (!ph.pair0) take_class(0);
         take_class(1);
         take_class(2);
         take_class(3);
@@ -432,34 +457,56 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
             };
             add_ctrl(g.control);
             add_ctrl(g.control2);
+            if (o.creg) o.flags |= OPF_CREG;
+            if (o.cout) o.flags |= OPF_COUT;
             const int lt = loc[g.target];
             const int rt = lt >= 0 ? reg_of_local[lt] : -1;
             if (diag[i]) {
-                o.d0_is_one = (g.mat[0] == 1.0 && g.mat[1] == 0.0) ? 1 : 0;
-                if (g.mat[6] == 1.0 && g.mat[7] == 0.0 && o.d0_is_one) continue;  // identity
+                const bool d0one = g.mat[0] == 1.0 && g.mat[1] == 0.0;
+                if (d0one) o.flags |= OPF_D0_ONE;
+                if (d0one && g.mat[6] == 1.0 && g.mat[7] == 0.0) continue;  // identity
                 if (rt >= 0) {
-                    o.kind = OP_DREG;
                     o.tbit = (uint8_t)rt;
+                    o.kind = (d0one && g.mat[6] == -1.0 && g.mat[7] == 0.0) ? OP_NEGHI : OP_DREG;
                 } else {
                     o.kind = OP_DOUT;
                     o.tout = uint64_t(1) << g.target;
+                    if (o.creg == 0) ph.flags |= PHF_ACC;
                 }
             } else {
                 o.tbit = (uint8_t)rt;
                 const bool real = g.mat[1] == 0 && g.mat[3] == 0 && g.mat[5] == 0 && g.mat[7] == 0;
-                if (is_x_like(g))
+                const bool imoff = g.mat[1] == 0 && g.mat[7] == 0 && g.mat[2] == 0 && g.mat[4] == 0;
+                const int had = hadamard_like(g);
+                if (is_x_like(g)) {
                     o.kind = OP_X;
-                else if (real)
+                } else if (rt >= 1 && o.creg == 0 && o.cout == 0 && had >= 0) {
+                    o.kind = (uint8_t)had;  // runs without its 1/sqrt2: deferred
+                    pending_scale *= rsqrt2;
+                    pending_count++;
+                } else if (rt >= 1 && o.creg == 0 && real) {
                     o.kind = OP_REAL;
-                else
+                } else if (rt >= 1 && o.creg == 0 && imoff) {
+                    o.kind = OP_IMOFF;
+                } else {
                     o.kind = OP_U;
+                }
             }
             prog.ops.push_back(o);
         }
         ph.op_end = (uint32_t)prog.ops.size();
-        prog.phases.push_back(ph);
         for (int i : members) done[i] = 1;
         ndone += members.size();
+        // apply the deferred factors before they could leave FP32 range
+        // (2^(count/2) growth), and always at the last phase
+        const bool last = ndone == gates.size();
+        ph.scale = 1.0f;
+        if (pending_count > 0 && (last || pending_count >= 48)) {
+            ph.scale = (float)pending_scale;
+            pending_scale = 1.0;
+            pending_count = 0;
+        }
+        prog.phases.push_back(ph);
     }
     return prog;
 }

@@ -22,38 +22,57 @@ struct PlainGate {
 };
 
 // ---- OShareMem tile program ------------------------------------------------
-// Op kinds applied to the amplitudes a thread holds in registers.
+// In a phase every thread holds 32 amplitudes over 5 "register qubits".
+// Register index i: bit 0 = the tile's local qubit 0 (physical qubit 0),
+// always a register qubit and the lane of the packed f32x2 vectors; bits 1..4
+// = four more tile qubits chosen per phase.  Amplitudes are kept as
+// structure-of-arrays vectors: re[j] = (re(2j), re(2j+1)), im[j] likewise.
 enum OshmOpKind : uint8_t {
-    OP_U = 0,       // general 2x2 on register bit `tbit`
-    OP_X = 1,       // exchange lo/hi on register bit `tbit`
-    OP_DREG = 2,    // diag(d0,d1) with register target bit `tbit` (d0 = m[0..1], d1 = m[6..7])
-    OP_DOUT = 3,    // diag(d0,d1) whose target is outside the register set (physical `tout`)
-    OP_RY = 4,      // real 2x2 [[a,-b],[b,a]] on `tbit` (RY, H-like real rotations use OP_REAL)
-    OP_REAL = 5     // real 2x2 (m00r m01r m10r m11r in m[0],m[2],m[4],m[6])
+    OP_U = 0,      // general complex 2x2 (m = re00 im00 re01 im01 re10 im10 re11 im11)
+    OP_REAL = 1,   // real 2x2 (m0, m2, m4, m6)
+    OP_IMOFF = 2,  // [[a, i b], [i c, d]], a, b, c, d real (m0, m3, m5, m6)
+    OP_H = 3,      // (1/sqrt2) [[1, 1], [1, -1]], scale deferred
+    OP_SY = 4,     // (1/sqrt2) [[1, -1], [1, 1]], scale deferred (RY(pi/2))
+    OP_SX = 5,     // (1/sqrt2) [[1, -i], [-i, 1]], scale deferred (RX(pi/2))
+    OP_X = 6,      // exchange lo/hi
+    OP_DREG = 7,   // diag(d0, d1) on a register qubit (d0 = m0 m1, d1 = m6 m7)
+    OP_NEGHI = 8,  // diag(1, -1) on a register qubit (Z, CZ)
+    OP_DOUT = 9    // diag(d0, d1) whose target is outside the register set
+};
+enum OshmOpFlags : uint8_t {
+    OPF_D0_ONE = 1,   // diagonal op: d0 == 1
+    OPF_COUT = 2,     // has controls outside the register set (`cout`)
+    OPF_CREG = 4      // has controls on register qubits (`creg`)
 };
 
-struct OshmOp {
+struct alignas(16) OshmOp {
     uint8_t kind;
-    uint8_t tbit;
-    uint8_t d0_is_one;  // OP_DREG/OP_DOUT: d0 == 1, lo untouched
-    uint8_t pad;
+    uint8_t tbit;       // register-index bit of the target (0..4)
+    uint8_t flags;
+    uint8_t pad0;
     uint32_t creg;      // register-index control mask
     uint64_t cout;      // physical control mask outside the register set
     uint64_t tout;      // OP_DOUT: physical target bit
+    uint64_t pad1;
     float m[8];
 };
-static_assert(sizeof(OshmOp) == 56, "OshmOp layout");
+static_assert(sizeof(OshmOp) == 64, "OshmOp layout");
 
 constexpr int OSHM_MAX_R = 5;      // register bits per thread (32 amplitudes)
 constexpr int OSHM_MAX_K = 13;     // tile bits
 constexpr int OSHM_MAX_G = OSHM_MAX_K;  // thread-index bits
 
+enum OshmPhaseFlags : uint8_t {
+    PHF_ACC = 1     // apply the per-thread phase accumulated by OP_DOUT ops
+};
+
 struct alignas(16) OshmPhase {
     uint32_t op_begin, op_end;
-    uint8_t r_local[OSHM_MAX_R];  // local tile bit of register bit j
+    uint8_t r_local[OSHM_MAX_R];  // local tile bit of register bit j (r_local[0] == 0)
     uint8_t g_local[OSHM_MAX_G];  // local tile bit of thread-index bit j
     uint8_t g_phys[OSHM_MAX_G];   // physical bit of thread-index bit j
-    uint8_t pair0;                // local bit 0 is register bit 0 (16-byte smem accesses)
+    uint8_t flags;
+    float scale;                  // real factor applied at the end of the phase (deferred 1/sqrt2's)
 };
 static_assert(sizeof(OshmPhase) == 48, "OshmPhase layout");
 

@@ -13,6 +13,12 @@
 //     group into PHASES: in a phase every thread holds 2^R amplitudes (R = 5,
 //     the phase's "register qubits") in registers and applies all the phase's
 //     gates there; only one shared-memory round trip per phase.
+//   * Registers hold structure-of-arrays f32x2 vectors pairing the two
+//     amplitudes that differ in physical qubit 0, so the gate arithmetic runs
+//     on Blackwell's packed FFMA2/FADD2/FMUL2 (two amplitudes per instruction).
+//   * Hadamard-like gates (H, sqrt(X) = RX(pi/2), sqrt(Y) = RY(pi/2)) run as
+//     adds/subtracts; their 1/sqrt(2) factors are collected by the host and
+//     applied as one multiply per phase that needs it.
 //   * Tiles are staged with 16-byte cp.async copies (LDGSTS), whose 2^c-amplitude
 //     runs over the lowest physical qubits are coalesced; shared memory is
 //     XOR-swizzled (linear map S below) so the phase gathers are conflict-free
@@ -30,237 +36,474 @@ namespace {
 
 __host__ __device__ __forceinline__ uint32_t swz(uint32_t x) { return tile_swz(x); }
 
+// packed f32x2 arithmetic (FFMA2 / FADD2 / FMUL2 on sm_100+)
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 swp(float2 a) { return make_float2(a.y, a.x); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-template <int J, int NR>
-__device__ __forceinline__ void op_u(float2 (&v)[NR], const float (&m)[8], uint32_t creg) {
-#pragma unroll
-    for (int i = 0; i < NR; i++) {
-        if (i & (1 << J)) continue;
-        if ((uint32_t(i) & creg) != creg) continue;
-        const int h = i | (1 << J);
-        const float2 a = v[i], b = v[h];
-        v[i].x = m[0] * a.x - m[1] * a.y + m[2] * b.x - m[3] * b.y;
-        v[i].y = m[0] * a.y + m[1] * a.x + m[2] * b.y + m[3] * b.x;
-        v[h].x = m[4] * a.x - m[5] * a.y + m[6] * b.x - m[7] * b.y;
-        v[h].y = m[4] * a.y + m[5] * a.x + m[6] * b.y + m[7] * b.x;
+// Amplitudes of one thread: register index i = 2 j + lane, vectors
+// re[j] = (re(2j), re(2j+1)), im[j] likewise.  Register bit J >= 1 is bit
+// J-1 of the vector index; register bit 0 is the lane.
+template <int NV>
+struct Amps {
+    float2 re[NV], im[NV];
+};
+
+// ---- uncontrolled ops on register bit J >= 1 --------------------------------
+#define HQ_PAIRS(J, NV, BODY)                              \
+    _Pragma("unroll") for (int j = 0; j < NV; j++) {        \
+        if (j & (1 << (J - 1))) continue;                    \
+        const int h = j | (1 << (J - 1));                    \
+        const float2 lr = A.re[j], li = A.im[j], hr = A.re[h], hi = A.im[h]; \
+        BODY                                                 \
     }
+
+template <int J, int NV>
+__device__ __forceinline__ void op_u(Amps<NV>& A, const float (&m)[8]) {
+    const float2 a = f2(m[0]), ai = f2(m[1]), ain = f2(-m[1]);
+    const float2 b = f2(m[2]), bi = f2(m[3]), bin = f2(-m[3]);
+    const float2 c = f2(m[4]), ci = f2(m[5]), cin = f2(-m[5]);
+    const float2 d = f2(m[6]), di = f2(m[7]), din = f2(-m[7]);
+    HQ_PAIRS(J, NV, {
+        A.re[j] = fma2(bin, hi, fma2(b, hr, fma2(ain, li, mul2(a, lr))));
+        A.im[j] = fma2(bi, hr, fma2(b, hi, fma2(ai, lr, mul2(a, li))));
+        A.re[h] = fma2(din, hi, fma2(d, hr, fma2(cin, li, mul2(c, lr))));
+        A.im[h] = fma2(di, hr, fma2(d, hi, fma2(ci, lr, mul2(c, li))));
+    })
 }
 
-// real 2x2: [[m0, m2], [m4, m6]]
-template <int J, int NR>
-__device__ __forceinline__ void op_real(float2 (&v)[NR], const float (&m)[8], uint32_t creg) {
-#pragma unroll
-    for (int i = 0; i < NR; i++) {
-        if (i & (1 << J)) continue;
-        if ((uint32_t(i) & creg) != creg) continue;
-        const int h = i | (1 << J);
-        const float2 a = v[i], b = v[h];
-        v[i].x = m[0] * a.x + m[2] * b.x;
-        v[i].y = m[0] * a.y + m[2] * b.y;
-        v[h].x = m[4] * a.x + m[6] * b.x;
-        v[h].y = m[4] * a.y + m[6] * b.y;
-    }
+template <int J, int NV>
+__device__ __forceinline__ void op_real(Amps<NV>& A, const float (&m)[8]) {
+    const float2 a = f2(m[0]), b = f2(m[2]), c = f2(m[4]), d = f2(m[6]);
+    HQ_PAIRS(J, NV, {
+        A.re[j] = fma2(b, hr, mul2(a, lr));
+        A.im[j] = fma2(b, hi, mul2(a, li));
+        A.re[h] = fma2(d, hr, mul2(c, lr));
+        A.im[h] = fma2(d, hi, mul2(c, li));
+    })
 }
 
-template <int J, int NR>
-__device__ __forceinline__ void op_x(float2 (&v)[NR], uint32_t creg) {
-#pragma unroll
-    for (int i = 0; i < NR; i++) {
-        if (i & (1 << J)) continue;
-        if ((uint32_t(i) & creg) != creg) continue;
-        const int h = i | (1 << J);
-        const float2 a = v[i];
-        v[i] = v[h];
-        v[h] = a;
-    }
+// [[a, i b], [i c, d]]
+template <int J, int NV>
+__device__ __forceinline__ void op_imoff(Amps<NV>& A, const float (&m)[8]) {
+    const float2 a = f2(m[0]), b = f2(m[3]), bn = f2(-m[3]), c = f2(m[5]), cn = f2(-m[5]),
+                 d = f2(m[6]);
+    HQ_PAIRS(J, NV, {
+        A.re[j] = fma2(bn, hi, mul2(a, lr));
+        A.im[j] = fma2(b, hr, mul2(a, li));
+        A.re[h] = fma2(cn, li, mul2(d, hr));
+        A.im[h] = fma2(c, lr, mul2(d, hi));
+    })
 }
 
-template <int J, int NR>
-__device__ __forceinline__ void op_dreg(float2 (&v)[NR], const float (&m)[8], uint32_t creg,
-                                        bool d0_is_one) {
-    const float2 d0 = make_float2(m[0], m[1]), d1 = make_float2(m[6], m[7]);
-#pragma unroll
-    for (int i = 0; i < NR; i++) {
-        if ((uint32_t(i) & creg) != creg) continue;
-        if (i & (1 << J)) {
-            v[i] = cmul(v[i], d1);
-        } else if (!d0_is_one) {
-            v[i] = cmul(v[i], d0);
+template <int J, int NV>
+__device__ __forceinline__ void op_h(Amps<NV>& A) {
+    HQ_PAIRS(J, NV, {
+        A.re[j] = add2(lr, hr);
+        A.im[j] = add2(li, hi);
+        A.re[h] = sub2(lr, hr);
+        A.im[h] = sub2(li, hi);
+    })
+}
+
+template <int J, int NV>
+__device__ __forceinline__ void op_sy(Amps<NV>& A) {
+    HQ_PAIRS(J, NV, {
+        A.re[j] = sub2(lr, hr);
+        A.im[j] = sub2(li, hi);
+        A.re[h] = add2(lr, hr);
+        A.im[h] = add2(li, hi);
+    })
+}
+
+template <int J, int NV>
+__device__ __forceinline__ void op_sx(Amps<NV>& A) {
+    HQ_PAIRS(J, NV, {
+        A.re[j] = add2(lr, hi);
+        A.im[j] = sub2(li, hr);
+        A.re[h] = add2(hr, li);
+        A.im[h] = sub2(hi, lr);
+    })
+}
+
+template <int J, int NV>
+__device__ __forceinline__ void op_x(Amps<NV>& A) {
+    HQ_PAIRS(J, NV, {
+        A.re[j] = hr;
+        A.im[j] = hi;
+        A.re[h] = lr;
+        A.im[h] = li;
+    })
+}
+
+template <int J, int NV>
+__device__ __forceinline__ void op_dreg(Amps<NV>& A, const float (&m)[8], bool d0one) {
+    const float2 er = f2(m[6]), ei = f2(m[7]), ein = f2(-m[7]);
+    const float2 fr = f2(m[0]), fi = f2(m[1]), fin = f2(-m[1]);
+    HQ_PAIRS(J, NV, {
+        A.re[h] = fma2(ein, hi, mul2(er, hr));
+        A.im[h] = fma2(ei, hr, mul2(er, hi));
+        if (!d0one) {
+            A.re[j] = fma2(fin, li, mul2(fr, lr));
+            A.im[j] = fma2(fi, lr, mul2(fr, li));
         }
-    }
+    })
 }
 
-template <int NR>
-__device__ __forceinline__ void op_scale(float2 (&v)[NR], float2 f, uint32_t creg) {
+template <int J, int NV>
+__device__ __forceinline__ void op_neghi(Amps<NV>& A) {
+    const float2 n1 = f2(-1.f);
+    HQ_PAIRS(J, NV, {
+        (void)lr;
+        (void)li;
+        A.re[h] = mul2(n1, hr);
+        A.im[h] = mul2(n1, hi);
+    })
+}
+
+// ---- ops on register bit 0 (the vector lane: lo = .x, hi = .y) ------------------
+template <int NV>
+__device__ __forceinline__ void lane_u(Amps<NV>& A, const float (&m)[8], uint32_t creg) {
+    const float2 P = make_float2(m[0], m[6]), Q = make_float2(m[1], m[7]);
+    const float2 Qn = make_float2(-m[1], -m[7]);
+    const float2 S = make_float2(m[2], m[4]), Tt = make_float2(m[3], m[5]);
+    const float2 Tn = make_float2(-m[3], -m[5]);
 #pragma unroll
-    for (int i = 0; i < NR; i++) {
-        if ((uint32_t(i) & creg) != creg) continue;
-        v[i] = cmul(v[i], f);
+    for (int j = 0; j < NV; j++) {
+        if ((uint32_t(2 * j) & creg) != creg) continue;
+        const float2 r = A.re[j], i = A.im[j], rs = swp(r), is = swp(i);
+        A.re[j] = fma2(Tn, is, fma2(S, rs, fma2(Qn, i, mul2(P, r))));
+        A.im[j] = fma2(Tt, rs, fma2(S, is, fma2(Q, r, mul2(P, i))));
     }
 }
 
-#define HQ_DISPATCH_TBIT(R, TBIT, CALL)                 \
-    switch (TBIT) {                                     \
-        case 0: { constexpr int J = 0; CALL; } break;   \
-        case 1: if constexpr (R > 1) { constexpr int J = 1; CALL; } break; \
-        case 2: if constexpr (R > 2) { constexpr int J = 2; CALL; } break; \
-        case 3: if constexpr (R > 3) { constexpr int J = 3; CALL; } break; \
-        case 4: if constexpr (R > 4) { constexpr int J = 4; CALL; } break; \
-        default: break;                                 \
+template <int NV>
+__device__ __forceinline__ void lane_x(Amps<NV>& A, uint32_t creg) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+        if ((uint32_t(2 * j) & creg) != creg) continue;
+        A.re[j] = swp(A.re[j]);
+        A.im[j] = swp(A.im[j]);
     }
+}
+
+template <int NV>
+__device__ __forceinline__ void lane_diag(Amps<NV>& A, const float (&m)[8], uint32_t creg) {
+    const float2 R = make_float2(m[0], m[6]), I = make_float2(m[1], m[7]);
+    const float2 In = make_float2(-m[1], -m[7]);
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+        if ((uint32_t(2 * j) & creg) != creg) continue;
+        const float2 r = A.re[j], i = A.im[j];
+        A.re[j] = fma2(In, i, mul2(R, r));
+        A.im[j] = fma2(I, r, mul2(R, i));
+    }
+}
+
+// ---- register-controlled ops on bit J >= 1: compute, then keep per lane ----------
+__device__ __forceinline__ float2 pick(bool o0, bool o1, float2 nw, float2 old) {
+    return make_float2(o0 ? nw.x : old.x, o1 ? nw.y : old.y);
+}
+
+template <int J, int NV>
+__device__ __forceinline__ void ctl_u(Amps<NV>& A, const float (&m)[8], uint32_t creg) {
+    const float2 a = f2(m[0]), ai = f2(m[1]), ain = f2(-m[1]);
+    const float2 b = f2(m[2]), bi = f2(m[3]), bin = f2(-m[3]);
+    const float2 c = f2(m[4]), ci = f2(m[5]), cin = f2(-m[5]);
+    const float2 d = f2(m[6]), di = f2(m[7]), din = f2(-m[7]);
+    HQ_PAIRS(J, NV, {
+        const bool o0 = (uint32_t(2 * j) & creg) == creg;
+        const bool o1 = (uint32_t(2 * j + 1) & creg) == creg;
+        A.re[j] = pick(o0, o1, fma2(bin, hi, fma2(b, hr, fma2(ain, li, mul2(a, lr)))), lr);
+        A.im[j] = pick(o0, o1, fma2(bi, hr, fma2(b, hi, fma2(ai, lr, mul2(a, li)))), li);
+        A.re[h] = pick(o0, o1, fma2(din, hi, fma2(d, hr, fma2(cin, li, mul2(c, lr)))), hr);
+        A.im[h] = pick(o0, o1, fma2(di, hr, fma2(d, hi, fma2(ci, lr, mul2(c, li)))), hi);
+    })
+}
+
+template <int J, int NV>
+__device__ __forceinline__ void ctl_x(Amps<NV>& A, uint32_t creg) {
+    HQ_PAIRS(J, NV, {
+        const bool o0 = (uint32_t(2 * j) & creg) == creg;
+        const bool o1 = (uint32_t(2 * j + 1) & creg) == creg;
+        A.re[j] = pick(o0, o1, hr, lr);
+        A.im[j] = pick(o0, o1, hi, li);
+        A.re[h] = pick(o0, o1, lr, hr);
+        A.im[h] = pick(o0, o1, li, hi);
+    })
+}
+
+template <int J, int NV>
+__device__ __forceinline__ void ctl_diag(Amps<NV>& A, const float (&m)[8], uint32_t creg,
+                                         bool d0one) {
+    HQ_PAIRS(J, NV, {
+        const bool o0 = (uint32_t(2 * j) & creg) == creg;
+        const bool o1 = (uint32_t(2 * j + 1) & creg) == creg;
+        const float2 er = make_float2(o0 ? m[6] : 1.f, o1 ? m[6] : 1.f);
+        const float2 ei = make_float2(o0 ? m[7] : 0.f, o1 ? m[7] : 0.f);
+        A.re[h] = fma2(make_float2(-ei.x, -ei.y), hi, mul2(er, hr));
+        A.im[h] = fma2(ei, hr, mul2(er, hi));
+        if (!d0one) {
+            const float2 fr = make_float2(o0 ? m[0] : 1.f, o1 ? m[0] : 1.f);
+            const float2 fi = make_float2(o0 ? m[1] : 0.f, o1 ? m[1] : 0.f);
+            A.re[j] = fma2(make_float2(-fi.x, -fi.y), li, mul2(fr, lr));
+            A.im[j] = fma2(fi, lr, mul2(fr, li));
+        }
+    })
+}
+
+// multiply the registers selected by creg by the complex factor f
+template <int NV>
+__device__ __forceinline__ void scale_sel(Amps<NV>& A, float2 f, uint32_t creg) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+        const bool o0 = (uint32_t(2 * j) & creg) == creg;
+        const bool o1 = (uint32_t(2 * j + 1) & creg) == creg;
+        if (!o0 && !o1) continue;
+        const float2 R = make_float2(o0 ? f.x : 1.f, o1 ? f.x : 1.f);
+        const float2 I = make_float2(o0 ? f.y : 0.f, o1 ? f.y : 0.f);
+        const float2 r = A.re[j], i = A.im[j];
+        A.re[j] = fma2(make_float2(-I.x, -I.y), i, mul2(R, r));
+        A.im[j] = fma2(I, r, mul2(R, i));
+    }
+}
+
+#define HQ_TBIT(R, TB, CALL)                                                     \
+    switch (TB) {                                                                \
+        case 1: if constexpr (R > 1) { constexpr int J = 1; CALL; } break;       \
+        case 2: if constexpr (R > 2) { constexpr int J = 2; CALL; } break;       \
+        case 3: if constexpr (R > 3) { constexpr int J = 3; CALL; } break;       \
+        case 4: if constexpr (R > 4) { constexpr int J = 4; CALL; } break;       \
+        default: break;                                                          \
+    }
+
+template <int R>
+__device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hdr,
+                                         const OshmOp* __restrict__ op, uint64_t pidx,
+                                         float2& acc) {
+    constexpr int NV = 1 << (R - 1);
+    const uint32_t kind = hdr.x & 0xffu, tb = (hdr.x >> 8) & 0xffu, flags = (hdr.x >> 16) & 0xffu;
+    const uint32_t creg = hdr.y;
+    if (flags & OPF_COUT) {
+        const uint64_t cout = (uint64_t(hdr.w) << 32) | hdr.z;
+        if ((pidx & cout) != cout) return;
+    }
+    float m[8];
+    if (kind != OP_H && kind != OP_SY && kind != OP_SX && kind != OP_X && kind != OP_NEGHI) {
+        const float4* mp = reinterpret_cast<const float4*>(op->m);
+        const float4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
+        m[0] = m0.x; m[1] = m0.y; m[2] = m0.z; m[3] = m0.w;
+        m[4] = m1.x; m[5] = m1.y; m[6] = m1.z; m[7] = m1.w;
+    } else {
+#pragma unroll
+        for (int q = 0; q < 8; q++) m[q] = 0.f;
+    }
+    const bool d0one = (flags & OPF_D0_ONE) != 0;
+    if (kind == OP_DOUT) {
+        const uint64_t tout = __ldg(reinterpret_cast<const unsigned long long*>(&op->tout));
+        const bool hiset = (pidx & tout) != 0;
+        if (!hiset && d0one) return;
+        const float2 f = hiset ? make_float2(m[6], m[7]) : make_float2(m[0], m[1]);
+        if (creg == 0)
+            acc = cmul(acc, f);
+        else
+            scale_sel<NV>(A, f, creg);
+        return;
+    }
+    if (tb == 0) {
+        if (kind == OP_X)
+            lane_x<NV>(A, creg);
+        else if (kind == OP_DREG || kind == OP_NEGHI) {
+            if (kind == OP_NEGHI) {
+                m[0] = 1.f; m[1] = 0.f; m[6] = -1.f; m[7] = 0.f;
+            }
+            lane_diag<NV>(A, m, creg);
+        } else {
+            lane_u<NV>(A, m, creg);
+        }
+        return;
+    }
+    if (flags & OPF_CREG) {
+        switch (kind) {
+            case OP_X: HQ_TBIT(R, tb, (ctl_x<J, NV>(A, creg))); break;
+            case OP_NEGHI:
+                m[0] = 1.f; m[1] = 0.f; m[6] = -1.f; m[7] = 0.f;
+                HQ_TBIT(R, tb, (ctl_diag<J, NV>(A, m, creg, true)));
+                break;
+            case OP_DREG: HQ_TBIT(R, tb, (ctl_diag<J, NV>(A, m, creg, d0one))); break;
+            default: HQ_TBIT(R, tb, (ctl_u<J, NV>(A, m, creg))); break;
+        }
+        return;
+    }
+    switch (kind) {
+        case OP_U: HQ_TBIT(R, tb, (op_u<J, NV>(A, m))); break;
+        case OP_REAL: HQ_TBIT(R, tb, (op_real<J, NV>(A, m))); break;
+        case OP_IMOFF: HQ_TBIT(R, tb, (op_imoff<J, NV>(A, m))); break;
+        case OP_H: HQ_TBIT(R, tb, (op_h<J, NV>(A))); break;
+        case OP_SY: HQ_TBIT(R, tb, (op_sy<J, NV>(A))); break;
+        case OP_SX: HQ_TBIT(R, tb, (op_sx<J, NV>(A))); break;
+        case OP_X: HQ_TBIT(R, tb, (op_x<J, NV>(A))); break;
+        case OP_DREG: HQ_TBIT(R, tb, (op_dreg<J, NV>(A, m, d0one))); break;
+        case OP_NEGHI: HQ_TBIT(R, tb, (op_neghi<J, NV>(A))); break;
+        default: break;
+    }
+}
 
 template <int K, int R>
 __global__ void __launch_bounds__(1 << (K - R)) k_oshm(const OshmLaunch p) {
     constexpr int T = 1 << (K - R);      // threads per tile
-    constexpr int NR = 1 << R;           // amplitudes per thread in a phase
+    constexpr int NV = 1 << (R - 1);     // f32x2 vectors per thread (2 amplitudes each)
     constexpr int PPT = (1 << (K - 1)) / T;  // 16-byte pieces per thread
     static_assert(PPT >= 1 && PPT <= 32, "piece count");
-    extern __shared__ float4 smem4[];
-    float2* sm = reinterpret_cast<float2*>(smem4);
+    constexpr int TILE4 = 1 << (K - 1);  // float4 pieces per tile buffer
+    extern __shared__ float4 smem4[];     // two tile buffers
     const int t = threadIdx.x;
     float2* __restrict__ state = reinterpret_cast<float2*>(p.state);
 
-    // Tile base: deposit the tile index into the non-tile (block) bits.
-    const uint64_t base = tile_base(blockIdx.x, p.nruns, p.run_src, p.run_dst, p.run_len);
-
-    // Stage the tile: piece (t + m*T) holds local amplitudes 2(t + m*T) and +1.
-    const uint64_t toff = local_to_phys(uint32_t(t) << 1, K, p.tile_phys);  // local index 2t
+    // Piece (t + m*T) of a tile holds local amplitudes 2(t + m*T) and +1.
+    const uint64_t toff = local_to_phys(uint32_t(t) << 1, K, p.tile_phys);
     const uint32_t tslot = swz(uint32_t(t) << 1);
-    const float2* __restrict__ gsrc = state + base + toff;
-    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
-#pragma unroll
-    for (int m = 0; m < PPT; m++) {
-        const uint32_t slot = tslot ^ p.piece_slot[m];
-        const float2* g = gsrc + p.piece_off[m];
-        cp_async16(sbase + slot * 8u, g);
-    }
-    cp_async_commit();
-    cp_async_wait_all();
-    __syncthreads();
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem4);
 
-    for (int ph = 0; ph < p.nphases; ph++) {
-        const OshmPhase P = p.phases[ph];
-        uint32_t gl = 0;
-        uint64_t gphys = 0;
+    // stage tile u into buffer b, as loaded: (re0, im0, re1, im1)
+    auto load_tile = [&](uint64_t u, int b) {
+        const uint64_t tb = tile_base(u, p.nruns, p.run_src, p.run_dst, p.run_len);
+        const float2* __restrict__ gsrc = state + tb + toff;
+        const uint32_t bb = sbase + uint32_t(b) * TILE4 * 16u;
 #pragma unroll
-        for (int j = 0; j < K - R; j++) {
-            if ((t >> j) & 1) {
-                gl |= 1u << P.g_local[j];
-                gphys |= uint64_t(1) << P.g_phys[j];
-            }
-        }
-        const uint64_t pidx = base | gphys;  // physical index of this thread's register 0
-        const uint32_t sb = swz(gl);
-        uint32_t col[R];
-#pragma unroll
-        for (int j = 0; j < R; j++) col[j] = swz(1u << P.r_local[j]);
+        for (int m = 0; m < PPT; m++)
+            cp_async16(bb + (tslot ^ p.piece_slot[m]) * 8u, gsrc + p.piece_off[m]);
+        cp_async_commit();
+    };
 
-        float2 v[NR];
-        if (P.pair0) {
-#pragma unroll
-            for (int i = 0; i < NR; i += 2) {
-                uint32_t s = sb;
-#pragma unroll
-                for (int j = 1; j < R; j++)
-                    if ((i >> j) & 1) s ^= col[j];
-                const float4 q = smem4[s >> 1];
-                v[i] = make_float2(q.x, q.y);
-                v[i + 1] = make_float2(q.z, q.w);
-            }
+    // Persistent loop over tiles; the next tile's copy is in flight while the
+    // current one is computed.
+    uint64_t u = blockIdx.x;
+    if (u < p.ntiles) load_tile(u, 0);
+    for (int it = 0; u < p.ntiles; it++, u += gridDim.x) {
+        const uint64_t un = u + gridDim.x;
+        if (un < p.ntiles) {
+            load_tile(un, (it + 1) & 1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         } else {
-#pragma unroll
-            for (int i = 0; i < NR; i++) {
-                uint32_t s = sb;
-#pragma unroll
-                for (int j = 0; j < R; j++)
-                    if ((i >> j) & 1) s ^= col[j];
-                v[i] = sm[s];
-            }
-        }
-
-        float2 acc = make_float2(1.f, 0.f);
-        for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) {
-            const OshmOp& o = p.ops[oi];
-            const uint8_t kind = o.kind;
-            const uint32_t creg = o.creg;
-            const uint64_t cout = o.cout;
-            if ((pidx & cout) != cout) continue;
-            float m[8];
-#pragma unroll
-            for (int q = 0; q < 8; q++) m[q] = o.m[q];
-            const int tb = o.tbit;
-            switch (kind) {
-                case OP_U: HQ_DISPATCH_TBIT(R, tb, (op_u<J, NR>(v, m, creg))); break;
-                case OP_REAL: HQ_DISPATCH_TBIT(R, tb, (op_real<J, NR>(v, m, creg))); break;
-                case OP_X: HQ_DISPATCH_TBIT(R, tb, (op_x<J, NR>(v, creg))); break;
-                case OP_DREG: {
-                    const bool d0one = o.d0_is_one != 0;
-                    HQ_DISPATCH_TBIT(R, tb, (op_dreg<J, NR>(v, m, creg, d0one)));
-                    break;
-                }
-                case OP_DOUT: {
-                    const bool hi = (pidx & o.tout) != 0;
-                    if (!hi && o.d0_is_one) break;
-                    const float2 f = hi ? make_float2(m[6], m[7]) : make_float2(m[0], m[1]);
-                    if (creg == 0)
-                        acc = cmul(acc, f);
-                    else
-                        op_scale<NR>(v, f, creg);
-                    break;
-                }
-                default: break;
-            }
-        }
-        if (acc.x != 1.f || acc.y != 0.f) op_scale<NR>(v, acc, 0u);
-
-        if (P.pair0) {
-#pragma unroll
-            for (int i = 0; i < NR; i += 2) {
-                uint32_t s = sb;
-#pragma unroll
-                for (int j = 1; j < R; j++)
-                    if ((i >> j) & 1) s ^= col[j];
-                smem4[s >> 1] = make_float4(v[i].x, v[i].y, v[i + 1].x, v[i + 1].y);
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < NR; i++) {
-                uint32_t s = sb;
-#pragma unroll
-                for (int j = 0; j < R; j++)
-                    if ((i >> j) & 1) s ^= col[j];
-                sm[s] = v[i];
-            }
+            cp_async_wait_all();
         }
         __syncthreads();
-    }
+        float4* buf = smem4 + (it & 1) * TILE4;
+        const uint64_t base = tile_base(u, p.nruns, p.run_src, p.run_dst, p.run_len);
 
-    // Write the tile back in place.
-    float2* __restrict__ gdst = state + base + toff;
+        for (int ph = 0; ph < p.nphases; ph++) {
+            const OshmPhase P = p.phases[ph];
+            uint32_t gl = 0;
+            uint64_t gphys = 0;
 #pragma unroll
-    for (int m = 0; m < PPT; m++) {
-        const uint32_t slot = tslot ^ p.piece_slot[m];
-        const float4 q = smem4[slot >> 1];
-        *reinterpret_cast<float4*>(gdst + p.piece_off[m]) = q;
+            for (int j = 0; j < K - R; j++) {
+                if ((t >> j) & 1) {
+                    gl |= 1u << P.g_local[j];
+                    gphys |= uint64_t(1) << P.g_phys[j];
+                }
+            }
+            const uint64_t pidx = base | gphys;  // physical index of register 0
+            const uint32_t sb = swz(gl);
+            uint32_t col[R];
+#pragma unroll
+            for (int j = 1; j < R; j++) col[j] = swz(1u << P.r_local[j]);
+
+            Amps<NV> A;
+            // gather: pieces are (re0, im0, re1, im1) before the first phase and
+            // (re0, re1, im0, im1) after it
+#pragma unroll
+            for (int j = 0; j < NV; j++) {
+                uint32_t s = sb;
+#pragma unroll
+                for (int b = 1; b < R; b++)
+                    if ((j >> (b - 1)) & 1) s ^= col[b];
+                const float4 q = buf[s >> 1];
+                if (ph == 0) {
+                    A.re[j] = make_float2(q.x, q.z);
+                    A.im[j] = make_float2(q.y, q.w);
+                } else {
+                    A.re[j] = make_float2(q.x, q.y);
+                    A.im[j] = make_float2(q.z, q.w);
+                }
+            }
+
+            float2 acc = make_float2(1.f, 0.f);
+            const OshmOp* __restrict__ ops = p.ops;
+            uint4 nxt = make_uint4(0, 0, 0, 0);
+            if (P.op_begin < P.op_end) nxt = __ldg(reinterpret_cast<const uint4*>(ops + P.op_begin));
+            for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) {
+                const uint4 hdr = nxt;
+                if (oi + 1 < P.op_end) nxt = __ldg(reinterpret_cast<const uint4*>(ops + oi + 1));
+                apply_op<R>(A, hdr, ops + oi, pidx, acc);
+            }
+            float2 f = acc;
+            if (P.scale != 1.f) f = make_float2(f.x * P.scale, f.y * P.scale);
+            if (f.y != 0.f) {
+                const float2 R2 = f2(f.x), I2 = f2(f.y), In2 = f2(-f.y);
+#pragma unroll
+                for (int j = 0; j < NV; j++) {
+                    const float2 r = A.re[j], i = A.im[j];
+                    A.re[j] = fma2(In2, i, mul2(R2, r));
+                    A.im[j] = fma2(I2, r, mul2(R2, i));
+                }
+            } else if (f.x != 1.f) {
+                const float2 R2 = f2(f.x);
+#pragma unroll
+                for (int j = 0; j < NV; j++) {
+                    A.re[j] = mul2(R2, A.re[j]);
+                    A.im[j] = mul2(R2, A.im[j]);
+                }
+            }
+
+#pragma unroll
+            for (int j = 0; j < NV; j++) {
+                uint32_t s = sb;
+#pragma unroll
+                for (int b = 1; b < R; b++)
+                    if ((j >> (b - 1)) & 1) s ^= col[b];
+                buf[s >> 1] = make_float4(A.re[j].x, A.re[j].y, A.im[j].x, A.im[j].y);
+            }
+            __syncthreads();
+        }
+
+        // write back in place, (re0, re1, im0, im1) -> (re0, im0, re1, im1)
+        float2* __restrict__ gdst = state + base + toff;
+        const bool soa = p.nphases > 0;
+#pragma unroll
+        for (int m = 0; m < PPT; m++) {
+            const float4 q = buf[(tslot ^ p.piece_slot[m]) >> 1];
+            *reinterpret_cast<float4*>(gdst + p.piece_off[m]) =
+                soa ? make_float4(q.x, q.z, q.y, q.w) : q;
+        }
+        __syncthreads();  // this buffer is refilled two iterations on
     }
 }
 
 template <int K, int R>
 void launch_k(const OshmLaunch& p, cudaStream_t s) {
     constexpr int T = 1 << (K - R);
-    const size_t smem = sizeof(float2) << K;
-    static bool attr_set = false;
-    if (!attr_set) {
+    const size_t smem = 2 * (sizeof(float2) << K);  // double-buffered tile
+    static int blocks_per_sm = 0;
+    if (!blocks_per_sm) {
         HQ_CHECK_CUDA(cudaFuncSetAttribute(k_oshm<K, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
-        attr_set = true;
+        HQ_CHECK_CUDA(
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_oshm<K, R>, T, smem));
+        HQ_REQUIRE(blocks_per_sm >= 1, HQ_ERR_UNSUPPORTED, "oshm<%d>: does not fit on an SM", K);
     }
-    HQ_REQUIRE(p.ntiles >= 1 && p.ntiles <= 0x7fffffffull, HQ_ERR_INVALID, "oshm: %llu tiles",
-               (unsigned long long)p.ntiles);
-    k_oshm<K, R><<<(unsigned)p.ntiles, T, smem, s>>>(p);
+    HQ_REQUIRE(p.ntiles >= 1, HQ_ERR_INVALID, "oshm: no tiles");
+    const uint64_t slots = uint64_t(ctx().sm_count) * blocks_per_sm;
+    const unsigned grid = (unsigned)(p.ntiles < slots ? p.ntiles : slots);
+    k_oshm<K, R><<<grid, T, smem, s>>>(p);
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 
