@@ -511,14 +511,16 @@ void launch_k(const OshmLaunch& p, cudaStream_t s) {
 
 uint32_t oshm_swizzle(uint32_t x) { return swz(x); }
 
-int oshm_reg_bits(int k) { return k >= 10 ? 5 : (k > 5 ? k - 5 : 1); }
+// register bits per tile width: 5 from 10 tile qubits up; at least 2 so that a
+// phase always has a register qubit besides the f32x2 lane
+int oshm_reg_bits(int k) { return k >= 10 ? 5 : (k >= 7 ? k - 5 : 2); }
 
 int oshm_threads(int k, int r) { return 1 << (k - r); }
 
 void launch_oshm(const OshmLaunch& p, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     switch (p.k) {
-        case 6: launch_k<6, 1>(p, s); break;
+        case 6: launch_k<6, 2>(p, s); break;
         case 7: launch_k<7, 2>(p, s); break;
         case 8: launch_k<8, 3>(p, s); break;
         case 9: launch_k<9, 4>(p, s); break;
