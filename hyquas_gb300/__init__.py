@@ -54,7 +54,7 @@ class hq_gate(C.Structure):
 class hq_compile_options(C.Structure):
     _fields_ = [("backend", C.c_int32), ("tile_qubits", C.c_int32), ("coalesce", C.c_int32),
                 ("mm_qubits", C.c_int32), ("mm_precision", C.c_int32),
-                ("reference_grouping", C.c_int32)]
+                ("reference_grouping", C.c_int32), ("specialize", C.c_int32)]
 
 
 def _load():
@@ -408,7 +408,8 @@ class Circuit:
         check(lib.hq_circuit_add_gates(self._h, arr, len(gates)))
 
     def compile(self, backend: str | int = "oshm", tile_qubits: int = 0, coalesce: int = 0,
-                mm_qubits: int = 0, precision: str | int = "bf16x3", reference_grouping: bool = False):
+                mm_qubits: int = 0, precision: str | int = "bf16x3", reference_grouping: bool = False,
+                specialize: int = 2):
         o = hq_compile_options()
         check(lib.hq_compile_options_default(C.byref(o)))
         o.backend = _BACKENDS[backend] if isinstance(backend, str) else backend
@@ -417,6 +418,7 @@ class Circuit:
         o.mm_qubits = mm_qubits
         o.mm_precision = _PRECISIONS[precision] if isinstance(precision, str) else precision
         o.reference_grouping = 1 if reference_grouping else 0
+        o.specialize = specialize
         check(lib.hq_circuit_compile(self._h, C.byref(o)))
 
     def schedule(self):

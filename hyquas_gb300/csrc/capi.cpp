@@ -247,6 +247,7 @@ hq_status hq_compile_options_default(hq_compile_options* opt) {
     std::memset(opt, 0, sizeof(*opt));
     opt->backend = HQ_BACKEND_OSHM;
     opt->mm_precision = HQ_MM_BF16X3;
+    opt->specialize = 2;
     HQ_API_END
 }
 

@@ -305,12 +305,39 @@ void circuit_compile(hq_circuit_s* c, const hq_compile_options& o) {
     }
     transmm_finalize(c);
     HQ_CHECK_CUDA(cudaStreamSynchronize(st));
+    c->specialized = false;
+    c->specialize_note.clear();
+    if (o.specialize != 0) {
+        std::vector<const OshmProgram*> progs;
+        std::vector<size_t> idx;
+        for (size_t i = 0; i < c->dgroups.size(); i++)
+            if (c->dgroups[i].backend == HQ_BACKEND_OSHM) {
+                progs.push_back(&c->dgroups[i].prog);
+                idx.push_back(i);
+            }
+        if (!progs.empty()) {
+            try {
+                HQ_REQUIRE(jit_available(), HQ_ERR_UNSUPPORTED, "NVRTC not available");
+                std::vector<JitKernel> ks = jit_compile_groups(progs);
+                for (size_t i = 0; i < idx.size(); i++) {
+                    c->dgroups[idx[i]].jit = ks[i];
+                    c->dgroups[idx[i]].has_jit = true;
+                }
+                c->specialized = true;
+            } catch (const Failure& f) {
+                if (o.specialize == 1) throw;
+                c->specialize_note = f.what();  // auto mode: the interpreter runs these groups
+            }
+        }
+    }
     c->compiled = true;
 }
 
 void circuit_launch_groups(hq_circuit_s* c, void* state, cudaStream_t st) {
     for (const DeviceGroup& dg : c->dgroups) {
-        if (dg.backend == HQ_BACKEND_OSHM) {
+        if (dg.backend == HQ_BACKEND_OSHM && dg.has_jit) {
+            jit_launch(dg.jit, state, uint64_t(1) << (c->n - dg.prog.k), st);
+        } else if (dg.backend == HQ_BACKEND_OSHM) {
             OshmLaunch p = make_oshm_launch(dg.prog, state, c->d_phases + dg.phase_off,
                                             c->d_ops, ctx().d_error);
             launch_oshm(p, st);
@@ -360,7 +387,9 @@ void circuit_profile(hq_circuit_s* c, hq_state_s* s, double* group_us) {
     HQ_CHECK_CUDA(cudaEventRecord(ev[0], st));
     for (size_t g = 0; g < ng; g++) {
         const DeviceGroup& dg = c->dgroups[g];
-        if (dg.backend == HQ_BACKEND_OSHM) {
+        if (dg.backend == HQ_BACKEND_OSHM && dg.has_jit) {
+            jit_launch(dg.jit, s->d, uint64_t(1) << (c->n - dg.prog.k), st);
+        } else if (dg.backend == HQ_BACKEND_OSHM) {
             OshmLaunch p = make_oshm_launch(dg.prog, s->d, c->d_phases + dg.phase_off, c->d_ops,
                                             ctx().d_error);
             launch_oshm(p, st);

@@ -5,9 +5,11 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
 #include <vector>
 
 #include "compiler.h"
+#include "jit.h"
 
 struct hq_state_s {
     int n = 0;
@@ -33,6 +35,8 @@ struct DeviceGroup {
     size_t umat_off = 0;         // offset (doubles) of the FP64 fused unitary
     size_t operand_off = 0;      // offset (bytes) of the precision-specific operand
     std::vector<hq_gate> phys_gates;
+    bool has_jit = false;        // a generated kernel replaces the interpreter
+    JitKernel jit;
 };
 
 }  // namespace hq
@@ -59,6 +63,8 @@ struct hq_circuit_s {
     cudaGraphExec_t graph = nullptr;
     const hq_state_s* graph_state = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool specialized = false;           // OShareMem groups run generated kernels
+    std::string specialize_note;        // why not, when requested in auto mode
 };
 
 namespace hq {

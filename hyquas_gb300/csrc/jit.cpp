@@ -1,0 +1,603 @@
+// Specialised OShareMem kernels: one straight-line kernel per gate group.
+//
+// The interpreter kernel (k_oshm.cu) runs any group, but every op pays a
+// dispatch and, because 64 live amplitude registers cross a dynamic op loop,
+// register copies at each iteration.  For a compiled circuit the group is
+// known in full, so this file writes the group as CUDA C++ -- tile bits,
+// gathers, every op with its matrix as literals, register controls resolved
+// per amplitude at generation time -- and compiles it with NVRTC for sm_103a
+// (loaded through the runtime's library API).  The tile framework (persistent
+// CTAs, double-buffered cp.async staging, swizzled shared memory, f32x2 math)
+// is the interpreter's; only the op stream becomes straight-line code.
+//
+// NVRTC is opened at run time; when it is missing, compile falls back to the
+// interpreter kernel (both are GPU paths).
+#include "jit.h"
+
+#include <dlfcn.h>
+
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <thread>
+
+#include "common.h"
+
+namespace hq {
+
+// ---- NVRTC entry points (dlopen) ----------------------------------------------
+namespace {
+
+typedef int nvrtcResult_t;
+typedef struct _nvrtcProgram* nvrtcProgram_t;
+struct Nvrtc {
+    bool ok = false;
+    std::string why;
+    nvrtcResult_t (*create)(nvrtcProgram_t*, const char*, const char*, int, const char* const*,
+                            const char* const*) = nullptr;
+    nvrtcResult_t (*compile)(nvrtcProgram_t, int, const char* const*) = nullptr;
+    nvrtcResult_t (*log_size)(nvrtcProgram_t, size_t*) = nullptr;
+    nvrtcResult_t (*log)(nvrtcProgram_t, char*) = nullptr;
+    nvrtcResult_t (*cubin_size)(nvrtcProgram_t, size_t*) = nullptr;
+    nvrtcResult_t (*cubin)(nvrtcProgram_t, char*) = nullptr;
+    nvrtcResult_t (*destroy)(nvrtcProgram_t*) = nullptr;
+};
+
+Nvrtc& nvrtc() {
+    static Nvrtc n;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char* cands[] = {"libnvrtc.so.13", "libnvrtc.so",
+                               "/usr/local/cuda/lib64/libnvrtc.so.13",
+                               "/usr/local/cuda/targets/sbsa-linux/lib/libnvrtc.so.13",
+                               "/usr/local/cuda/targets/x86_64-linux/lib/libnvrtc.so.13"};
+        void* h = nullptr;
+        if (const char* home = getenv("CUDA_HOME")) {
+            std::string p = std::string(home) + "/lib64/libnvrtc.so.13";
+            h = dlopen(p.c_str(), RTLD_NOW | RTLD_LOCAL);
+        }
+        for (const char* c : cands) {
+            if (h) break;
+            h = dlopen(c, RTLD_NOW | RTLD_LOCAL);
+        }
+        if (!h) {
+            n.why = "libnvrtc.so.13 not found";
+            return;
+        }
+        n.create = (decltype(n.create))dlsym(h, "nvrtcCreateProgram");
+        n.compile = (decltype(n.compile))dlsym(h, "nvrtcCompileProgram");
+        n.log_size = (decltype(n.log_size))dlsym(h, "nvrtcGetProgramLogSize");
+        n.log = (decltype(n.log))dlsym(h, "nvrtcGetProgramLog");
+        n.cubin_size = (decltype(n.cubin_size))dlsym(h, "nvrtcGetCUBINSize");
+        n.cubin = (decltype(n.cubin))dlsym(h, "nvrtcGetCUBIN");
+        n.destroy = (decltype(n.destroy))dlsym(h, "nvrtcDestroyProgram");
+        n.ok = n.create && n.compile && n.log_size && n.log && n.cubin_size && n.cubin && n.destroy;
+        if (!n.ok) n.why = "libnvrtc.so.13 lacks the expected symbols";
+    });
+    return n;
+}
+
+// ---- source generation -----------------------------------------------------------
+
+const char* kPrelude = R"(
+typedef unsigned long long v2;
+typedef unsigned long long u64;
+#define DI __device__ __forceinline__
+DI v2 vadd(v2 a, v2 b) { v2 d; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d; }
+DI v2 vsub(v2 a, v2 b) { v2 d; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d; }
+DI v2 vmul(v2 a, v2 b) { v2 d; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d; }
+DI v2 vfma(v2 a, v2 b, v2 c) { v2 d; asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c)); return d; }
+DI v2 vpack(float lo, float hi) { v2 d; asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi)); return d; }
+DI void vunpack(v2 a, float& lo, float& hi) { asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a)); }
+DI v2 vdup(float x) { return vpack(x, x); }
+DI v2 vswap(v2 a) { float l, h; vunpack(a, l, h); return vpack(h, l); }
+DI v2 vlane(v2 nw, v2 old, bool k0, bool k1) { float a, b, c, d; vunpack(nw, a, b); vunpack(old, c, d); return vpack(k0 ? a : c, k1 ? b : d); }
+DI float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+DI unsigned swz(unsigned x) { unsigned f = ((x >> 4) ^ (x >> 7) ^ (x >> 10) ^ (x >> 13)) & 7u; return x ^ (f << 1); }
+DI void cpa16(unsigned s, const void* g) { asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(g) : "memory"); }
+DI float F(unsigned b) { return __int_as_float((int)b); }
+)";
+
+std::string flit(float f) {
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    char buf[32];
+    snprintf(buf, sizeof(buf), "F(0x%08xu)", b);
+    return buf;
+}
+
+std::string hex64(uint64_t x) {
+    char buf[32];
+    snprintf(buf, sizeof(buf), "0x%llxull", (unsigned long long)x);
+    return buf;
+}
+
+uint32_t swz_host(uint32_t x) {
+    const uint32_t f = ((x >> 4) ^ (x >> 7) ^ (x >> 10) ^ (x >> 13)) & 7u;
+    return x ^ (f << 1);
+}
+
+struct Gen {
+    std::ostringstream o;
+    int nv = 16;
+    int tmp = 0;
+    std::string t(const char* p) { return std::string(p) + std::to_string(tmp++); }
+    static std::string R(int j) { return "r" + std::to_string(j); }
+    static std::string I(int j) { return "i" + std::to_string(j); }
+
+    // lane-control mask for the vector pair starting at j: ok lanes
+    static void lanes(uint32_t creg, int j, bool& k0, bool& k1) {
+        k0 = ((uint32_t(2 * j)) & creg) == creg;
+        k1 = ((uint32_t(2 * j + 1)) & creg) == creg;
+    }
+
+    void assign(const std::string& dst, const std::string& expr, const std::string& old, bool k0,
+                bool k1) {
+        if (k0 && k1)
+            o << dst << " = " << expr << ";\n";
+        else if (k0 || k1)
+            o << dst << " = vlane(" << expr << ", " << old << ", " << (k0 ? "true" : "false") << ", "
+              << (k1 ? "true" : "false") << ");\n";
+    }
+
+    void op(const OshmOp& op, bool& uses_acc) {
+        const int kind = op.kind, J = op.tbit;
+        const float* m = op.m;
+        const bool has_cout = (op.flags & OPF_COUT) != 0;
+        if (has_cout) o << "if ((pidx & " << hex64(op.cout) << ") == " << hex64(op.cout) << ") {\n";
+        o << "{\n";
+        if (kind == OP_DOUT) {
+            const bool d0one = (op.flags & OPF_D0_ONE) != 0;
+            o << "const bool hb = (pidx & " << hex64(op.tout) << ") != 0ull;\n";
+            o << "const float2 f = hb ? make_float2(" << flit(m[6]) << ", " << flit(m[7])
+              << ") : make_float2(" << flit(m[0]) << ", " << flit(m[1]) << ");\n";
+            if (op.creg == 0) {
+                uses_acc = true;
+                if (d0one)
+                    o << "if (hb) acc = cmul(acc, f);\n";
+                else
+                    o << "acc = cmul(acc, f);\n";
+            } else {
+                o << "const v2 fr = vdup(f.x), fi = vdup(f.y), fin = vdup(-f.y);\n";
+                for (int j = 0; j < nv; j++) {
+                    bool k0, k1;
+                    lanes(op.creg, j, k0, k1);
+                    if (!k0 && !k1) continue;
+                    o << "{ const v2 a = " << R(j) << ", b = " << I(j) << ";\n";
+                    assign(R(j), "vfma(fin, b, vmul(fr, a))", R(j), k0, k1);
+                    assign(I(j), "vfma(fi, a, vmul(fr, b))", I(j), k0, k1);
+                    o << "}\n";
+                }
+            }
+            o << "}\n";
+            if (has_cout) o << "}\n";
+            return;
+        }
+        if (J == 0) {
+            // target = the vector lane
+            if (kind == OP_X) {
+                for (int j = 0; j < nv; j++) {
+                    if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
+                    o << R(j) << " = vswap(" << R(j) << "); " << I(j) << " = vswap(" << I(j) << ");\n";
+                }
+            } else if (kind == OP_DREG || kind == OP_NEGHI) {
+                float d0r = m[0], d0i = m[1], d1r = m[6], d1i = m[7];
+                if (kind == OP_NEGHI) {
+                    d0r = 1.f; d0i = 0.f; d1r = -1.f; d1i = 0.f;
+                }
+                o << "const v2 Rr = vpack(" << flit(d0r) << ", " << flit(d1r) << "), Ii = vpack("
+                  << flit(d0i) << ", " << flit(d1i) << "), In = vpack(" << flit(-d0i) << ", "
+                  << flit(-d1i) << ");\n";
+                for (int j = 0; j < nv; j++) {
+                    if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
+                    o << "{ const v2 a = " << R(j) << ", b = " << I(j) << "; " << R(j)
+                      << " = vfma(In, b, vmul(Rr, a)); " << I(j) << " = vfma(Ii, a, vmul(Rr, b)); }\n";
+                }
+            } else {
+                o << "const v2 P = vpack(" << flit(m[0]) << ", " << flit(m[6]) << "), Q = vpack("
+                  << flit(m[1]) << ", " << flit(m[7]) << "), Qn = vpack(" << flit(-m[1]) << ", "
+                  << flit(-m[7]) << "), S = vpack(" << flit(m[2]) << ", " << flit(m[4])
+                  << "), T = vpack(" << flit(m[3]) << ", " << flit(m[5]) << "), Tn = vpack("
+                  << flit(-m[3]) << ", " << flit(-m[5]) << ");\n";
+                for (int j = 0; j < nv; j++) {
+                    if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
+                    o << "{ const v2 a = " << R(j) << ", b = " << I(j)
+                      << ", as = vswap(a), bs = vswap(b); " << R(j)
+                      << " = vfma(Tn, bs, vfma(S, as, vfma(Qn, b, vmul(P, a)))); " << I(j)
+                      << " = vfma(T, as, vfma(S, bs, vfma(Q, a, vmul(P, b)))); }\n";
+                }
+            }
+            o << "}\n";
+            if (has_cout) o << "}\n";
+            return;
+        }
+        // target = register bit J >= 1: vector pairs (j, j | 1 << (J-1))
+        auto consts = [&](const char* names[], const float* vals, int cnt) {
+            for (int q = 0; q < cnt; q++)
+                o << "const v2 " << names[q] << " = vdup(" << flit(vals[q]) << ");\n";
+        };
+        switch (kind) {
+            case OP_U: {
+                const char* nm[] = {"a", "ai", "ain", "b", "bi", "bin", "c", "ci", "cin", "d", "di", "din"};
+                const float v[] = {m[0], m[1], -m[1], m[2], m[3], -m[3], m[4], m[5], -m[5], m[6], m[7], -m[7]};
+                consts(nm, v, 12);
+                break;
+            }
+            case OP_REAL: {
+                const char* nm[] = {"a", "b", "c", "d"};
+                const float v[] = {m[0], m[2], m[4], m[6]};
+                consts(nm, v, 4);
+                break;
+            }
+            case OP_IMOFF: {
+                const char* nm[] = {"a", "b", "bn", "c", "cn", "d"};
+                const float v[] = {m[0], m[3], -m[3], m[5], -m[5], m[6]};
+                consts(nm, v, 6);
+                break;
+            }
+            case OP_DREG: {
+                const char* nm[] = {"er", "ei", "ein", "fr", "fi", "fin"};
+                const float v[] = {m[6], m[7], -m[7], m[0], m[1], -m[1]};
+                consts(nm, v, 6);
+                break;
+            }
+            case OP_NEGHI: {
+                const char* nm[] = {"n1"};
+                const float v[] = {-1.f};
+                consts(nm, v, 1);
+                break;
+            }
+            default: break;
+        }
+        const bool d0one = (op.flags & OPF_D0_ONE) != 0;
+        for (int j = 0; j < nv; j++) {
+            if (j & (1 << (J - 1))) continue;
+            const int h = j | (1 << (J - 1));
+            bool k0, k1;
+            lanes(op.creg, j, k0, k1);
+            if (!k0 && !k1) continue;
+            o << "{ const v2 lr = " << R(j) << ", li = " << I(j) << ", hr = " << R(h) << ", hi = " << I(h)
+              << ";\n";
+            switch (kind) {
+                case OP_U:
+                    assign(R(j), "vfma(bin, hi, vfma(b, hr, vfma(ain, li, vmul(a, lr))))", "lr", k0, k1);
+                    assign(I(j), "vfma(bi, hr, vfma(b, hi, vfma(ai, lr, vmul(a, li))))", "li", k0, k1);
+                    assign(R(h), "vfma(din, hi, vfma(d, hr, vfma(cin, li, vmul(c, lr))))", "hr", k0, k1);
+                    assign(I(h), "vfma(di, hr, vfma(d, hi, vfma(ci, lr, vmul(c, li))))", "hi", k0, k1);
+                    break;
+                case OP_REAL:
+                    assign(R(j), "vfma(b, hr, vmul(a, lr))", "lr", k0, k1);
+                    assign(I(j), "vfma(b, hi, vmul(a, li))", "li", k0, k1);
+                    assign(R(h), "vfma(d, hr, vmul(c, lr))", "hr", k0, k1);
+                    assign(I(h), "vfma(d, hi, vmul(c, li))", "hi", k0, k1);
+                    break;
+                case OP_IMOFF:
+                    assign(R(j), "vfma(bn, hi, vmul(a, lr))", "lr", k0, k1);
+                    assign(I(j), "vfma(b, hr, vmul(a, li))", "li", k0, k1);
+                    assign(R(h), "vfma(cn, li, vmul(d, hr))", "hr", k0, k1);
+                    assign(I(h), "vfma(c, lr, vmul(d, hi))", "hi", k0, k1);
+                    break;
+                case OP_H:
+                    assign(R(j), "vadd(lr, hr)", "lr", k0, k1);
+                    assign(I(j), "vadd(li, hi)", "li", k0, k1);
+                    assign(R(h), "vsub(lr, hr)", "hr", k0, k1);
+                    assign(I(h), "vsub(li, hi)", "hi", k0, k1);
+                    break;
+                case OP_SY:
+                    assign(R(j), "vsub(lr, hr)", "lr", k0, k1);
+                    assign(I(j), "vsub(li, hi)", "li", k0, k1);
+                    assign(R(h), "vadd(lr, hr)", "hr", k0, k1);
+                    assign(I(h), "vadd(li, hi)", "hi", k0, k1);
+                    break;
+                case OP_SX:
+                    assign(R(j), "vadd(lr, hi)", "lr", k0, k1);
+                    assign(I(j), "vsub(li, hr)", "li", k0, k1);
+                    assign(R(h), "vadd(hr, li)", "hr", k0, k1);
+                    assign(I(h), "vsub(hi, lr)", "hi", k0, k1);
+                    break;
+                case OP_X:
+                    assign(R(j), "hr", "lr", k0, k1);
+                    assign(I(j), "hi", "li", k0, k1);
+                    assign(R(h), "lr", "hr", k0, k1);
+                    assign(I(h), "li", "hi", k0, k1);
+                    break;
+                case OP_DREG:
+                    assign(R(h), "vfma(ein, hi, vmul(er, hr))", "hr", k0, k1);
+                    assign(I(h), "vfma(ei, hr, vmul(er, hi))", "hi", k0, k1);
+                    if (!d0one) {
+                        assign(R(j), "vfma(fin, li, vmul(fr, lr))", "lr", k0, k1);
+                        assign(I(j), "vfma(fi, lr, vmul(fr, li))", "li", k0, k1);
+                    }
+                    break;
+                case OP_NEGHI:
+                    assign(R(h), "vmul(n1, hr)", "hr", k0, k1);
+                    assign(I(h), "vmul(n1, hi)", "hi", k0, k1);
+                    break;
+                default: break;
+            }
+            o << "}\n";
+        }
+        o << "}\n";
+        if (has_cout) o << "}\n";
+    }
+};
+
+std::string deposit_expr(const char* var, uint32_t nbits, const uint8_t* dst, bool is64) {
+    std::ostringstream e;
+    e << "(";
+    bool first = true;
+    for (uint32_t j = 0; j < nbits; j++) {
+        if (!first) e << " | ";
+        first = false;
+        if (is64)
+            e << "((u64)((" << var << " >> " << j << ") & 1u) << " << int(dst[j]) << ")";
+        else
+            e << "((((unsigned)" << var << " >> " << j << ") & 1u) << " << int(dst[j]) << ")";
+    }
+    if (first) e << "0";
+    e << ")";
+    return e.str();
+}
+
+std::string generate(const OshmProgram& prog, int& threads, size_t& smem) {
+    const int K = prog.k, R = prog.r, NV = 1 << (R - 1);
+    const int T = 1 << (K - R);
+    const int PPT = (1 << (K - 1)) / T;
+    threads = T;
+    smem = 2 * (sizeof(float) * 2 << K);
+    const int n = prog.n;
+    uint8_t tile_phys[OSHM_MAX_K];
+    for (int b = 0, j = 0; b < n; b++)
+        if ((prog.tile_mask >> b) & 1) tile_phys[j++] = (uint8_t)b;
+
+    Gen g;
+    g.nv = NV;
+    std::ostringstream& o = g.o;
+    o << kPrelude;
+    o << "extern \"C\" __global__ void __launch_bounds__(" << T
+      << ") hq_oshm_group(float2* __restrict__ state, u64 ntiles) {\n";
+    o << "extern __shared__ float4 smem4[];\nconst unsigned t = threadIdx.x;\n";
+    // physical offset of local index 2t and its slot
+    {
+        uint8_t dst[OSHM_MAX_K];
+        for (int j = 0; j < K - R; j++) dst[j] = tile_phys[j + 1];
+        o << "const u64 toff = " << deposit_expr("t", K - R, dst, true) << ";\n";
+        o << "const unsigned tslot = swz(t << 1);\n";
+    }
+    o << "unsigned sbase; asm(\"{ .reg .u64 p; cvta.to.shared.u64 p, %1; cvt.u32.u64 %0, p; }\" : "
+         "\"=r\"(sbase) : \"l\"(smem4));\n";
+    // tile base: constant runs of block bits
+    o << "auto tile_base = [&](u64 u) -> u64 { return 0ull";
+    {
+        int src = 0;
+        for (int b = 0; b < n;) {
+            if ((prog.tile_mask >> b) & 1) {
+                b++;
+                continue;
+            }
+            int len = 0;
+            while (b + len < n && !((prog.tile_mask >> (b + len)) & 1)) len++;
+            o << " | (((u >> " << src << ") & " << hex64((uint64_t(1) << len) - 1) << ") << " << b << ")";
+            src += len;
+            b += len;
+        }
+    }
+    o << "; };\n";
+    // piece offsets/slots per m
+    std::vector<uint64_t> poff(PPT);
+    std::vector<uint32_t> pslot(PPT);
+    for (int m = 0; m < PPT; m++) {
+        const uint32_t local = uint32_t(2 * m * T);
+        uint64_t off = 0;
+        for (int j = 0; j < K; j++)
+            if ((local >> j) & 1) off |= uint64_t(1) << tile_phys[j];
+        poff[m] = off;
+        pslot[m] = swz_host(local);
+    }
+    o << "auto load_tile = [&](u64 u, int b) {\n"
+         "const float2* gsrc = state + tile_base(u) + toff;\n"
+      << "const unsigned bb = sbase + (unsigned)b * " << ((1u << (K - 1)) * 16u) << "u;\n";
+    for (int m = 0; m < PPT; m++)
+        o << "cpa16(bb + ((tslot ^ " << pslot[m] << "u) << 3), gsrc + " << hex64(poff[m]) << ");\n";
+    o << "asm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n};\n";
+    // per-phase thread constants (independent of the tile)
+    for (size_t p = 0; p < prog.phases.size(); p++) {
+        const OshmPhase& P = prog.phases[p];
+        o << "const unsigned sb" << p << " = swz(" << deposit_expr("t", K - R, P.g_local, false) << ");\n";
+        o << "const u64 gp" << p << " = " << deposit_expr("t", K - R, P.g_phys, true) << ";\n";
+    }
+    o << "u64 u = blockIdx.x;\nif (u < ntiles) load_tile(u, 0);\n";
+    o << "for (int it = 0; u < ntiles; it++, u += gridDim.x) {\n"
+         "const u64 un = u + gridDim.x;\n"
+         "if (un < ntiles) { load_tile(un, (it + 1) & 1); asm volatile(\"cp.async.wait_group 1;\\n\" ::: "
+         "\"memory\"); }\n"
+         "else { asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\"); }\n"
+         "__syncthreads();\n"
+      << "float4* buf = smem4 + (it & 1) * " << (1 << (K - 1)) << ";\n"
+      << "const u64 base = tile_base(u);\n";
+    o << "v2 ";
+    for (int j = 0; j < NV; j++) o << (j ? ", " : "") << "r" << j << ", i" << j;
+    o << ";\n";
+    for (size_t p = 0; p < prog.phases.size(); p++) {
+        const OshmPhase& P = prog.phases[p];
+        o << "{ // phase " << p << "\n";
+        o << "const u64 pidx = base | gp" << p << ";\n(void)pidx;\n";
+        uint32_t col[OSHM_MAX_R];
+        for (int j = 1; j < R; j++) col[j] = swz_host(1u << P.r_local[j]);
+        for (int j = 0; j < NV; j++) {
+            uint32_t c = 0;
+            for (int b = 1; b < R; b++)
+                if ((j >> (b - 1)) & 1) c ^= col[b];
+            if (p == 0)
+                o << "{ const float4 q = buf[(sb" << p << " ^ " << c << "u) >> 1]; r" << j
+                  << " = vpack(q.x, q.z); i" << j << " = vpack(q.y, q.w); }\n";
+            else
+                o << "{ const ulonglong2 q = ((const ulonglong2*)buf)[(sb" << p << " ^ " << c
+                  << "u) >> 1]; r" << j << " = q.x; i" << j << " = q.y; }\n";
+        }
+        o << "float2 acc = make_float2(1.f, 0.f);\n(void)acc;\n";
+        bool uses_acc = false;
+        for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) g.op(prog.ops[oi], uses_acc);
+        if (uses_acc || P.scale != 1.f) {
+            o << "{ float2 f = acc;\n";
+            if (P.scale != 1.f) o << "f.x *= " << flit(P.scale) << "; f.y *= " << flit(P.scale) << ";\n";
+            o << "const v2 fr = vdup(f.x), fi = vdup(f.y), fin = vdup(-f.y);\n";
+            if (uses_acc) {
+                for (int j = 0; j < NV; j++)
+                    o << "{ const v2 a = r" << j << ", b = i" << j << "; r" << j
+                      << " = vfma(fin, b, vmul(fr, a)); i" << j << " = vfma(fi, a, vmul(fr, b)); }\n";
+            } else {
+                for (int j = 0; j < NV; j++)
+                    o << "r" << j << " = vmul(fr, r" << j << "); i" << j << " = vmul(fr, i" << j << ");\n";
+            }
+            o << "}\n";
+        }
+        for (int j = 0; j < NV; j++) {
+            uint32_t c = 0;
+            for (int b = 1; b < R; b++)
+                if ((j >> (b - 1)) & 1) c ^= col[b];
+            o << "((ulonglong2*)buf)[(sb" << p << " ^ " << c << "u) >> 1] = make_ulonglong2(r" << j
+              << ", i" << j << ");\n";
+        }
+        o << "__syncthreads();\n}\n";
+    }
+    // write back in place; pieces are (re0, re1, im0, im1) after a phase
+    o << "float2* gdst = state + base + toff;\n";
+    for (int m = 0; m < PPT && prog.phases.empty(); m++)
+        o << "*(float4*)(gdst + " << hex64(poff[m]) << ") = buf[(tslot ^ " << pslot[m] << "u) >> 1];\n";
+    for (int m = 0; m < PPT && !prog.phases.empty(); m++) {
+        o << "{ const ulonglong2 q = ((const ulonglong2*)buf)[(tslot ^ " << pslot[m]
+          << "u) >> 1]; float4 w; vunpack(q.x, w.x, w.z); vunpack(q.y, w.y, w.w); *(float4*)(gdst + "
+          << hex64(poff[m]) << ") = w; }\n";
+    }
+    o << "__syncthreads();\n}\n}\n";
+    return o.str();
+}
+
+struct CacheEntry {
+    JitKernel k;
+    bool ok = false;
+    std::string err;
+};
+
+std::mutex g_cache_mu;
+std::map<std::string, std::shared_ptr<CacheEntry>> g_cache;
+
+JitKernel compile_source(const std::string& src, int threads, size_t smem) {
+    Nvrtc& nv = nvrtc();
+    HQ_REQUIRE(nv.ok, HQ_ERR_UNSUPPORTED, "NVRTC unavailable: %s", nv.why.c_str());
+    nvrtcProgram_t prog = nullptr;
+    HQ_REQUIRE(nv.create(&prog, src.c_str(), "hq_oshm_group.cu", 0, nullptr, nullptr) == 0,
+               HQ_ERR_UNSUPPORTED, "nvrtcCreateProgram failed");
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17"};
+    const int rc = nv.compile(prog, 2, opts);
+    if (rc != 0) {
+        size_t ls = 0;
+        nv.log_size(prog, &ls);
+        std::string log(ls, '\0');
+        nv.log(prog, &log[0]);
+        nv.destroy(&prog);
+        fail(HQ_ERR_UNSUPPORTED, "NVRTC compile failed (%d): %.800s", rc, log.c_str());
+    }
+    size_t cs = 0;
+    nv.cubin_size(prog, &cs);
+    std::vector<char> cubin(cs);
+    nv.cubin(prog, cubin.data());
+    nv.destroy(&prog);
+    JitKernel k;
+    HQ_CHECK_CUDA(cudaLibraryLoadData(&k.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+    HQ_CHECK_CUDA(cudaLibraryGetKernel(&k.kern, k.lib, "hq_oshm_group"));
+    k.threads = threads;
+    k.smem = smem;
+    HQ_CHECK_CUDA(cudaFuncSetAttribute((const void*)k.kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    int bps = 0;
+    HQ_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)k.kern, threads, smem));
+    HQ_REQUIRE(bps >= 1, HQ_ERR_UNSUPPORTED, "specialised kernel does not fit on an SM");
+    k.blocks_per_sm = bps;
+    return k;
+}
+
+}  // namespace
+
+bool jit_available() { return nvrtc().ok; }
+
+std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>& progs) {
+    ensure_init();
+    std::vector<std::string> srcs(progs.size());
+    std::vector<int> threads(progs.size());
+    std::vector<size_t> smem(progs.size());
+    for (size_t i = 0; i < progs.size(); i++) srcs[i] = generate(*progs[i], threads[i], smem[i]);
+    std::vector<std::shared_ptr<CacheEntry>> ents(progs.size());
+    std::vector<size_t> todo;
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        for (size_t i = 0; i < progs.size(); i++) {
+            auto it = g_cache.find(srcs[i]);
+            if (it != g_cache.end()) {
+                ents[i] = it->second;
+            } else {
+                ents[i] = std::make_shared<CacheEntry>();
+                g_cache[srcs[i]] = ents[i];
+                todo.push_back(i);
+            }
+        }
+    }
+    // NVRTC compiles in parallel; loading (cudaLibraryLoadData) needs the device
+    // current in each worker thread
+    const int dev = ctx().device;
+    std::vector<std::thread> pool;
+    std::mutex next_mu;
+    size_t next = 0;
+    const size_t nthreads = std::min<size_t>(todo.size(), std::max(1u, std::thread::hardware_concurrency()));
+    for (size_t w = 0; w < nthreads; w++) {
+        pool.emplace_back([&] {
+            cudaSetDevice(dev);
+            while (true) {
+                size_t k;
+                {
+                    std::lock_guard<std::mutex> lk(next_mu);
+                    if (next >= todo.size()) return;
+                    k = todo[next++];
+                }
+                try {
+                    ents[k]->k = compile_source(srcs[k], threads[k], smem[k]);
+                    ents[k]->ok = true;
+                } catch (const Failure& f) {
+                    ents[k]->err = f.what();
+                }
+            }
+        });
+    }
+    for (auto& th : pool) th.join();
+    std::vector<JitKernel> out;
+    for (size_t i = 0; i < progs.size(); i++) {
+        if (!ents[i]->ok) {
+            std::lock_guard<std::mutex> lk(g_cache_mu);
+            g_cache.erase(srcs[i]);
+            fail(HQ_ERR_UNSUPPORTED, "%s", ents[i]->err.empty() ? "specialisation failed"
+                                                               : ents[i]->err.c_str());
+        }
+        out.push_back(ents[i]->k);
+    }
+    return out;
+}
+
+void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, cudaStream_t st) {
+    const uint64_t slots = uint64_t(ctx().sm_count) * k.blocks_per_sm;
+    const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
+    void* args[] = {&state, &ntiles};
+    HQ_CHECK_CUDA(cudaLaunchKernel((const void*)k.kern, dim3(grid), dim3(k.threads), args, k.smem, st));
+}
+
+std::string jit_source(const OshmProgram& prog) {
+    int t;
+    size_t s;
+    return generate(prog, t, s);
+}
+
+}  // namespace hq

@@ -1,0 +1,28 @@
+// Straight-line (specialised) OShareMem kernels compiled per gate group with
+// NVRTC; see jit.cpp.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "compiler.h"
+
+namespace hq {
+
+struct JitKernel {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t kern = nullptr;
+    int threads = 0;
+    size_t smem = 0;
+    int blocks_per_sm = 1;
+};
+
+bool jit_available();
+// Compile (or fetch from the process-wide cache) one kernel per program.
+std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>& progs);
+void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, cudaStream_t st);
+std::string jit_source(const OshmProgram& prog);
+
+}  // namespace hq

@@ -36,15 +36,44 @@ namespace {
 
 __host__ __device__ __forceinline__ uint32_t swz(uint32_t x) { return tile_swz(x); }
 
-// packed f32x2 arithmetic (FFMA2 / FADD2 / FMUL2 on sm_100+)
-__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+// Packed f32x2 arithmetic on native 64-bit registers (PTX add/sub/mul/fma
+// .f32x2, sm_100+): a v2 holds two fp32 values and never round-trips
+// through a float pair.
+typedef unsigned long long v2;
+__device__ __forceinline__ v2 vadd(v2 a, v2 b) {
+    v2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
 }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 swp(float2 a) { return make_float2(a.y, a.x); }
+__device__ __forceinline__ v2 vsub(v2 a, v2 b) {
+    v2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ v2 vmul(v2 a, v2 b) {
+    v2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ v2 vfma(v2 a, v2 b, v2 c) {
+    v2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ v2 vpack(float lo, float hi) {
+    v2 d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ void vunpack(v2 a, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
+}
+__device__ __forceinline__ v2 vdup(float x) { return vpack(x, x); }
+__device__ __forceinline__ v2 vswap(v2 a) {
+    float l, h;
+    vunpack(a, l, h);
+    return vpack(h, l);
+}
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -54,7 +83,7 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 // J-1 of the vector index; register bit 0 is the lane.
 template <int NV>
 struct Amps {
-    float2 re[NV], im[NV];
+    v2 re[NV], im[NV];
 };
 
 // ---- uncontrolled ops on register bit J >= 1 --------------------------------
@@ -62,75 +91,75 @@ struct Amps {
     _Pragma("unroll") for (int j = 0; j < NV; j++) {        \
         if (j & (1 << (J - 1))) continue;                    \
         const int h = j | (1 << (J - 1));                    \
-        const float2 lr = A.re[j], li = A.im[j], hr = A.re[h], hi = A.im[h]; \
+        const v2 lr = A.re[j], li = A.im[j], hr = A.re[h], hi = A.im[h]; \
         BODY                                                 \
     }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_u(Amps<NV>& A, const float (&m)[8]) {
-    const float2 a = f2(m[0]), ai = f2(m[1]), ain = f2(-m[1]);
-    const float2 b = f2(m[2]), bi = f2(m[3]), bin = f2(-m[3]);
-    const float2 c = f2(m[4]), ci = f2(m[5]), cin = f2(-m[5]);
-    const float2 d = f2(m[6]), di = f2(m[7]), din = f2(-m[7]);
+    const v2 a = vdup(m[0]), ai = vdup(m[1]), ain = vdup(-m[1]);
+    const v2 b = vdup(m[2]), bi = vdup(m[3]), bin = vdup(-m[3]);
+    const v2 c = vdup(m[4]), ci = vdup(m[5]), cin = vdup(-m[5]);
+    const v2 d = vdup(m[6]), di = vdup(m[7]), din = vdup(-m[7]);
     HQ_PAIRS(J, NV, {
-        A.re[j] = fma2(bin, hi, fma2(b, hr, fma2(ain, li, mul2(a, lr))));
-        A.im[j] = fma2(bi, hr, fma2(b, hi, fma2(ai, lr, mul2(a, li))));
-        A.re[h] = fma2(din, hi, fma2(d, hr, fma2(cin, li, mul2(c, lr))));
-        A.im[h] = fma2(di, hr, fma2(d, hi, fma2(ci, lr, mul2(c, li))));
+        A.re[j] = vfma(bin, hi, vfma(b, hr, vfma(ain, li, vmul(a, lr))));
+        A.im[j] = vfma(bi, hr, vfma(b, hi, vfma(ai, lr, vmul(a, li))));
+        A.re[h] = vfma(din, hi, vfma(d, hr, vfma(cin, li, vmul(c, lr))));
+        A.im[h] = vfma(di, hr, vfma(d, hi, vfma(ci, lr, vmul(c, li))));
     })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_real(Amps<NV>& A, const float (&m)[8]) {
-    const float2 a = f2(m[0]), b = f2(m[2]), c = f2(m[4]), d = f2(m[6]);
+    const v2 a = vdup(m[0]), b = vdup(m[2]), c = vdup(m[4]), d = vdup(m[6]);
     HQ_PAIRS(J, NV, {
-        A.re[j] = fma2(b, hr, mul2(a, lr));
-        A.im[j] = fma2(b, hi, mul2(a, li));
-        A.re[h] = fma2(d, hr, mul2(c, lr));
-        A.im[h] = fma2(d, hi, mul2(c, li));
+        A.re[j] = vfma(b, hr, vmul(a, lr));
+        A.im[j] = vfma(b, hi, vmul(a, li));
+        A.re[h] = vfma(d, hr, vmul(c, lr));
+        A.im[h] = vfma(d, hi, vmul(c, li));
     })
 }
 
 // [[a, i b], [i c, d]]
 template <int J, int NV>
 __device__ __forceinline__ void op_imoff(Amps<NV>& A, const float (&m)[8]) {
-    const float2 a = f2(m[0]), b = f2(m[3]), bn = f2(-m[3]), c = f2(m[5]), cn = f2(-m[5]),
-                 d = f2(m[6]);
+    const v2 a = vdup(m[0]), b = vdup(m[3]), bn = vdup(-m[3]), c = vdup(m[5]), cn = vdup(-m[5]),
+             d = vdup(m[6]);
     HQ_PAIRS(J, NV, {
-        A.re[j] = fma2(bn, hi, mul2(a, lr));
-        A.im[j] = fma2(b, hr, mul2(a, li));
-        A.re[h] = fma2(cn, li, mul2(d, hr));
-        A.im[h] = fma2(c, lr, mul2(d, hi));
+        A.re[j] = vfma(bn, hi, vmul(a, lr));
+        A.im[j] = vfma(b, hr, vmul(a, li));
+        A.re[h] = vfma(cn, li, vmul(d, hr));
+        A.im[h] = vfma(c, lr, vmul(d, hi));
     })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_h(Amps<NV>& A) {
     HQ_PAIRS(J, NV, {
-        A.re[j] = add2(lr, hr);
-        A.im[j] = add2(li, hi);
-        A.re[h] = sub2(lr, hr);
-        A.im[h] = sub2(li, hi);
+        A.re[j] = vadd(lr, hr);
+        A.im[j] = vadd(li, hi);
+        A.re[h] = vsub(lr, hr);
+        A.im[h] = vsub(li, hi);
     })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_sy(Amps<NV>& A) {
     HQ_PAIRS(J, NV, {
-        A.re[j] = sub2(lr, hr);
-        A.im[j] = sub2(li, hi);
-        A.re[h] = add2(lr, hr);
-        A.im[h] = add2(li, hi);
+        A.re[j] = vsub(lr, hr);
+        A.im[j] = vsub(li, hi);
+        A.re[h] = vadd(lr, hr);
+        A.im[h] = vadd(li, hi);
     })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_sx(Amps<NV>& A) {
     HQ_PAIRS(J, NV, {
-        A.re[j] = add2(lr, hi);
-        A.im[j] = sub2(li, hr);
-        A.re[h] = add2(hr, li);
-        A.im[h] = sub2(hi, lr);
+        A.re[j] = vadd(lr, hi);
+        A.im[j] = vsub(li, hr);
+        A.re[h] = vadd(hr, li);
+        A.im[h] = vsub(hi, lr);
     })
 }
 
@@ -146,42 +175,40 @@ __device__ __forceinline__ void op_x(Amps<NV>& A) {
 
 template <int J, int NV>
 __device__ __forceinline__ void op_dreg(Amps<NV>& A, const float (&m)[8], bool d0one) {
-    const float2 er = f2(m[6]), ei = f2(m[7]), ein = f2(-m[7]);
-    const float2 fr = f2(m[0]), fi = f2(m[1]), fin = f2(-m[1]);
+    const v2 er = vdup(m[6]), ei = vdup(m[7]), ein = vdup(-m[7]);
+    const v2 fr = vdup(m[0]), fi = vdup(m[1]), fin = vdup(-m[1]);
     HQ_PAIRS(J, NV, {
-        A.re[h] = fma2(ein, hi, mul2(er, hr));
-        A.im[h] = fma2(ei, hr, mul2(er, hi));
+        A.re[h] = vfma(ein, hi, vmul(er, hr));
+        A.im[h] = vfma(ei, hr, vmul(er, hi));
         if (!d0one) {
-            A.re[j] = fma2(fin, li, mul2(fr, lr));
-            A.im[j] = fma2(fi, lr, mul2(fr, li));
+            A.re[j] = vfma(fin, li, vmul(fr, lr));
+            A.im[j] = vfma(fi, lr, vmul(fr, li));
         }
     })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_neghi(Amps<NV>& A) {
-    const float2 n1 = f2(-1.f);
+    const v2 n1 = vdup(-1.f);
     HQ_PAIRS(J, NV, {
         (void)lr;
         (void)li;
-        A.re[h] = mul2(n1, hr);
-        A.im[h] = mul2(n1, hi);
+        A.re[h] = vmul(n1, hr);
+        A.im[h] = vmul(n1, hi);
     })
 }
 
-// ---- ops on register bit 0 (the vector lane: lo = .x, hi = .y) ------------------
+// ---- ops on register bit 0 (the vector lane: lo = low half, hi = high half) -----
 template <int NV>
 __device__ __forceinline__ void lane_u(Amps<NV>& A, const float (&m)[8], uint32_t creg) {
-    const float2 P = make_float2(m[0], m[6]), Q = make_float2(m[1], m[7]);
-    const float2 Qn = make_float2(-m[1], -m[7]);
-    const float2 S = make_float2(m[2], m[4]), Tt = make_float2(m[3], m[5]);
-    const float2 Tn = make_float2(-m[3], -m[5]);
+    const v2 P = vpack(m[0], m[6]), Q = vpack(m[1], m[7]), Qn = vpack(-m[1], -m[7]);
+    const v2 S = vpack(m[2], m[4]), Tt = vpack(m[3], m[5]), Tn = vpack(-m[3], -m[5]);
 #pragma unroll
     for (int j = 0; j < NV; j++) {
         if ((uint32_t(2 * j) & creg) != creg) continue;
-        const float2 r = A.re[j], i = A.im[j], rs = swp(r), is = swp(i);
-        A.re[j] = fma2(Tn, is, fma2(S, rs, fma2(Qn, i, mul2(P, r))));
-        A.im[j] = fma2(Tt, rs, fma2(S, is, fma2(Q, r, mul2(P, i))));
+        const v2 r = A.re[j], i = A.im[j], rs = vswap(r), is = vswap(i);
+        A.re[j] = vfma(Tn, is, vfma(S, rs, vfma(Qn, i, vmul(P, r))));
+        A.im[j] = vfma(Tt, rs, vfma(S, is, vfma(Q, r, vmul(P, i))));
     }
 }
 
@@ -190,42 +217,46 @@ __device__ __forceinline__ void lane_x(Amps<NV>& A, uint32_t creg) {
 #pragma unroll
     for (int j = 0; j < NV; j++) {
         if ((uint32_t(2 * j) & creg) != creg) continue;
-        A.re[j] = swp(A.re[j]);
-        A.im[j] = swp(A.im[j]);
+        A.re[j] = vswap(A.re[j]);
+        A.im[j] = vswap(A.im[j]);
     }
 }
 
 template <int NV>
 __device__ __forceinline__ void lane_diag(Amps<NV>& A, const float (&m)[8], uint32_t creg) {
-    const float2 R = make_float2(m[0], m[6]), I = make_float2(m[1], m[7]);
-    const float2 In = make_float2(-m[1], -m[7]);
+    const v2 R = vpack(m[0], m[6]), I = vpack(m[1], m[7]), In = vpack(-m[1], -m[7]);
 #pragma unroll
     for (int j = 0; j < NV; j++) {
         if ((uint32_t(2 * j) & creg) != creg) continue;
-        const float2 r = A.re[j], i = A.im[j];
-        A.re[j] = fma2(In, i, mul2(R, r));
-        A.im[j] = fma2(I, r, mul2(R, i));
+        const v2 r = A.re[j], i = A.im[j];
+        A.re[j] = vfma(In, i, vmul(R, r));
+        A.im[j] = vfma(I, r, vmul(R, i));
     }
 }
 
 // ---- register-controlled ops on bit J >= 1: compute, then keep per lane ----------
-__device__ __forceinline__ float2 pick(bool o0, bool o1, float2 nw, float2 old) {
-    return make_float2(o0 ? nw.x : old.x, o1 ? nw.y : old.y);
+__device__ __forceinline__ v2 pick(bool o0, bool o1, v2 nw, v2 old) {
+    if (o0 && o1) return nw;
+    if (!o0 && !o1) return old;
+    float nl, nh, ol, oh;
+    vunpack(nw, nl, nh);
+    vunpack(old, ol, oh);
+    return vpack(o0 ? nl : ol, o1 ? nh : oh);
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void ctl_u(Amps<NV>& A, const float (&m)[8], uint32_t creg) {
-    const float2 a = f2(m[0]), ai = f2(m[1]), ain = f2(-m[1]);
-    const float2 b = f2(m[2]), bi = f2(m[3]), bin = f2(-m[3]);
-    const float2 c = f2(m[4]), ci = f2(m[5]), cin = f2(-m[5]);
-    const float2 d = f2(m[6]), di = f2(m[7]), din = f2(-m[7]);
+    const v2 a = vdup(m[0]), ai = vdup(m[1]), ain = vdup(-m[1]);
+    const v2 b = vdup(m[2]), bi = vdup(m[3]), bin = vdup(-m[3]);
+    const v2 c = vdup(m[4]), ci = vdup(m[5]), cin = vdup(-m[5]);
+    const v2 d = vdup(m[6]), di = vdup(m[7]), din = vdup(-m[7]);
     HQ_PAIRS(J, NV, {
         const bool o0 = (uint32_t(2 * j) & creg) == creg;
         const bool o1 = (uint32_t(2 * j + 1) & creg) == creg;
-        A.re[j] = pick(o0, o1, fma2(bin, hi, fma2(b, hr, fma2(ain, li, mul2(a, lr)))), lr);
-        A.im[j] = pick(o0, o1, fma2(bi, hr, fma2(b, hi, fma2(ai, lr, mul2(a, li)))), li);
-        A.re[h] = pick(o0, o1, fma2(din, hi, fma2(d, hr, fma2(cin, li, mul2(c, lr)))), hr);
-        A.im[h] = pick(o0, o1, fma2(di, hr, fma2(d, hi, fma2(ci, lr, mul2(c, li)))), hi);
+        A.re[j] = pick(o0, o1, vfma(bin, hi, vfma(b, hr, vfma(ain, li, vmul(a, lr)))), lr);
+        A.im[j] = pick(o0, o1, vfma(bi, hr, vfma(b, hi, vfma(ai, lr, vmul(a, li)))), li);
+        A.re[h] = pick(o0, o1, vfma(din, hi, vfma(d, hr, vfma(cin, li, vmul(c, lr)))), hr);
+        A.im[h] = pick(o0, o1, vfma(di, hr, vfma(d, hi, vfma(ci, lr, vmul(c, li)))), hi);
     })
 }
 
@@ -247,15 +278,17 @@ __device__ __forceinline__ void ctl_diag(Amps<NV>& A, const float (&m)[8], uint3
     HQ_PAIRS(J, NV, {
         const bool o0 = (uint32_t(2 * j) & creg) == creg;
         const bool o1 = (uint32_t(2 * j + 1) & creg) == creg;
-        const float2 er = make_float2(o0 ? m[6] : 1.f, o1 ? m[6] : 1.f);
-        const float2 ei = make_float2(o0 ? m[7] : 0.f, o1 ? m[7] : 0.f);
-        A.re[h] = fma2(make_float2(-ei.x, -ei.y), hi, mul2(er, hr));
-        A.im[h] = fma2(ei, hr, mul2(er, hi));
+        const v2 er = vpack(o0 ? m[6] : 1.f, o1 ? m[6] : 1.f);
+        const v2 ei = vpack(o0 ? m[7] : 0.f, o1 ? m[7] : 0.f);
+        const v2 ein = vpack(o0 ? -m[7] : 0.f, o1 ? -m[7] : 0.f);
+        A.re[h] = vfma(ein, hi, vmul(er, hr));
+        A.im[h] = vfma(ei, hr, vmul(er, hi));
         if (!d0one) {
-            const float2 fr = make_float2(o0 ? m[0] : 1.f, o1 ? m[0] : 1.f);
-            const float2 fi = make_float2(o0 ? m[1] : 0.f, o1 ? m[1] : 0.f);
-            A.re[j] = fma2(make_float2(-fi.x, -fi.y), li, mul2(fr, lr));
-            A.im[j] = fma2(fi, lr, mul2(fr, li));
+            const v2 fr = vpack(o0 ? m[0] : 1.f, o1 ? m[0] : 1.f);
+            const v2 fi = vpack(o0 ? m[1] : 0.f, o1 ? m[1] : 0.f);
+            const v2 fin = vpack(o0 ? -m[1] : 0.f, o1 ? -m[1] : 0.f);
+            A.re[j] = vfma(fin, li, vmul(fr, lr));
+            A.im[j] = vfma(fi, lr, vmul(fr, li));
         }
     })
 }
@@ -268,11 +301,12 @@ __device__ __forceinline__ void scale_sel(Amps<NV>& A, float2 f, uint32_t creg) 
         const bool o0 = (uint32_t(2 * j) & creg) == creg;
         const bool o1 = (uint32_t(2 * j + 1) & creg) == creg;
         if (!o0 && !o1) continue;
-        const float2 R = make_float2(o0 ? f.x : 1.f, o1 ? f.x : 1.f);
-        const float2 I = make_float2(o0 ? f.y : 0.f, o1 ? f.y : 0.f);
-        const float2 r = A.re[j], i = A.im[j];
-        A.re[j] = fma2(make_float2(-I.x, -I.y), i, mul2(R, r));
-        A.im[j] = fma2(I, r, mul2(R, i));
+        const v2 R = vpack(o0 ? f.x : 1.f, o1 ? f.x : 1.f);
+        const v2 I = vpack(o0 ? f.y : 0.f, o1 ? f.y : 0.f);
+        const v2 In = vpack(o0 ? -f.y : 0.f, o1 ? -f.y : 0.f);
+        const v2 r = A.re[j], i = A.im[j];
+        A.re[j] = vfma(In, i, vmul(R, r));
+        A.im[j] = vfma(I, r, vmul(R, i));
     }
 }
 
@@ -426,13 +460,14 @@ __global__ void __launch_bounds__(1 << (K - R)) k_oshm(const OshmLaunch p) {
 #pragma unroll
                 for (int b = 1; b < R; b++)
                     if ((j >> (b - 1)) & 1) s ^= col[b];
-                const float4 q = buf[s >> 1];
                 if (ph == 0) {
-                    A.re[j] = make_float2(q.x, q.z);
-                    A.im[j] = make_float2(q.y, q.w);
+                    const float4 q = buf[s >> 1];
+                    A.re[j] = vpack(q.x, q.z);
+                    A.im[j] = vpack(q.y, q.w);
                 } else {
-                    A.re[j] = make_float2(q.x, q.y);
-                    A.im[j] = make_float2(q.z, q.w);
+                    const ulonglong2 q = reinterpret_cast<const ulonglong2*>(buf)[s >> 1];
+                    A.re[j] = q.x;
+                    A.im[j] = q.y;
                 }
             }
 
@@ -448,19 +483,19 @@ __global__ void __launch_bounds__(1 << (K - R)) k_oshm(const OshmLaunch p) {
             float2 f = acc;
             if (P.scale != 1.f) f = make_float2(f.x * P.scale, f.y * P.scale);
             if (f.y != 0.f) {
-                const float2 R2 = f2(f.x), I2 = f2(f.y), In2 = f2(-f.y);
+                const v2 R2 = vdup(f.x), I2 = vdup(f.y), In2 = vdup(-f.y);
 #pragma unroll
                 for (int j = 0; j < NV; j++) {
-                    const float2 r = A.re[j], i = A.im[j];
-                    A.re[j] = fma2(In2, i, mul2(R2, r));
-                    A.im[j] = fma2(I2, r, mul2(R2, i));
+                    const v2 r = A.re[j], i = A.im[j];
+                    A.re[j] = vfma(In2, i, vmul(R2, r));
+                    A.im[j] = vfma(I2, r, vmul(R2, i));
                 }
             } else if (f.x != 1.f) {
-                const float2 R2 = f2(f.x);
+                const v2 R2 = vdup(f.x);
 #pragma unroll
                 for (int j = 0; j < NV; j++) {
-                    A.re[j] = mul2(R2, A.re[j]);
-                    A.im[j] = mul2(R2, A.im[j]);
+                    A.re[j] = vmul(R2, A.re[j]);
+                    A.im[j] = vmul(R2, A.im[j]);
                 }
             }
 
@@ -470,7 +505,7 @@ __global__ void __launch_bounds__(1 << (K - R)) k_oshm(const OshmLaunch p) {
 #pragma unroll
                 for (int b = 1; b < R; b++)
                     if ((j >> (b - 1)) & 1) s ^= col[b];
-                buf[s >> 1] = make_float4(A.re[j].x, A.re[j].y, A.im[j].x, A.im[j].y);
+                reinterpret_cast<ulonglong2*>(buf)[s >> 1] = make_ulonglong2(A.re[j], A.im[j]);
             }
             __syncthreads();
         }
@@ -480,9 +515,16 @@ __global__ void __launch_bounds__(1 << (K - R)) k_oshm(const OshmLaunch p) {
         const bool soa = p.nphases > 0;
 #pragma unroll
         for (int m = 0; m < PPT; m++) {
-            const float4 q = buf[(tslot ^ p.piece_slot[m]) >> 1];
-            *reinterpret_cast<float4*>(gdst + p.piece_off[m]) =
-                soa ? make_float4(q.x, q.z, q.y, q.w) : q;
+            const uint32_t piece = (tslot ^ p.piece_slot[m]) >> 1;
+            float4 out;
+            if (soa) {
+                const ulonglong2 q = reinterpret_cast<const ulonglong2*>(buf)[piece];
+                vunpack(q.x, out.x, out.z);
+                vunpack(q.y, out.y, out.w);
+            } else {
+                out = buf[piece];
+            }
+            *reinterpret_cast<float4*>(gdst + p.piece_off[m]) = out;
         }
         __syncthreads();  // this buffer is refilled two iterations on
     }

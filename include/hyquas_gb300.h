@@ -173,6 +173,9 @@ typedef struct hq_compile_options {
     int32_t mm_qubits;     /* TransMM group width (0 = autotuned, else 4..8) */
     int32_t mm_precision;  /* hq_mm_precision */
     int32_t reference_grouping; /* 1 = use the reference's widths (tile 10, coalesce 3, MAT 6) */
+    int32_t specialize;    /* OShareMem kernels: 0 = interpreter, 1 = one generated kernel per
+                              group (NVRTC, error if unavailable), 2 = generated when NVRTC is
+                              present, else interpreter (default) */
 } hq_compile_options;
 
 hq_status hq_compile_options_default(hq_compile_options* opt);
