@@ -404,7 +404,22 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
             members.push_back((int)i);
         }
         HQ_REQUIRE(!members.empty(), HQ_ERR_INVALID, "oshm: planner made no progress");
-        for (int b = 1; b < k && __builtin_popcount(rset) < r; b++) rset |= 1u << b;
+        // pad the register set with the tile qubits fewest of this phase's
+        // diagonal gates target (a diagonal gate off the register set is a
+        // per-thread scalar instead of a multiply per amplitude)
+        {
+            std::vector<int> score(k, 0);
+            for (int i : members)
+                if (diag[i] && loc[gates[i].target] >= 0) score[loc[gates[i].target]]++;
+            std::vector<int> cand;
+            for (int b = 1; b < k; b++)
+                if (!((rset >> b) & 1)) cand.push_back(b);
+            std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) { return score[a] < score[b]; });
+            for (int b : cand) {
+                if (__builtin_popcount(rset) >= r) break;
+                rset |= 1u << b;
+            }
+        }
 
         OshmPhase ph;
         std::memset(&ph, 0, sizeof(ph));

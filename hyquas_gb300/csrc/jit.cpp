@@ -144,6 +144,7 @@ struct Gen {
               << (k1 ? "true" : "false") << ");\n";
     }
 
+    bool uses_neg = false;  // phase has sign-only factors outside the register set
     void op(const OshmOp& op, bool& uses_acc) {
         const int kind = op.kind, J = op.tbit;
         const float* m = op.m;
@@ -152,10 +153,28 @@ struct Gen {
         o << "{\n";
         if (kind == OP_DOUT) {
             const bool d0one = (op.flags & OPF_D0_ONE) != 0;
+            const bool neg = d0one && m[6] == -1.f && m[7] == 0.f;
             o << "const bool hb = (pidx & " << hex64(op.tout) << ") != 0ull;\n";
+            if (neg && op.creg != 0) {
+                o << "if (hb) {\n";
+                for (int j = 0; j < nv; j++) {
+                    bool k0, k1;
+                    lanes(op.creg, j, k0, k1);
+                    if (!k0 && !k1) continue;
+                    const char* mask = k0 && k1 ? "0x8000000080000000ull"
+                                                : (k0 ? "0x80000000ull" : "0x8000000000000000ull");
+                    o << R(j) << " ^= " << mask << "; " << I(j) << " ^= " << mask << ";\n";
+                }
+                o << "}\n}\n";
+                if (has_cout) o << "}\n";
+                return;
+            }
             o << "const float2 f = hb ? make_float2(" << flit(m[6]) << ", " << flit(m[7])
               << ") : make_float2(" << flit(m[0]) << ", " << flit(m[1]) << ");\n";
-            if (op.creg == 0) {
+            if (op.creg == 0 && neg) {
+                uses_neg = true;
+                o << "if (hb) negf = !negf;\n";
+            } else if (op.creg == 0) {
                 uses_acc = true;
                 if (d0one)
                     o << "if (hb) acc = cmul(acc, f);\n";
@@ -184,11 +203,13 @@ struct Gen {
                     if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
                     o << R(j) << " = vswap(" << R(j) << "); " << I(j) << " = vswap(" << I(j) << ");\n";
                 }
-            } else if (kind == OP_DREG || kind == OP_NEGHI) {
-                float d0r = m[0], d0i = m[1], d1r = m[6], d1i = m[7];
-                if (kind == OP_NEGHI) {
-                    d0r = 1.f; d0i = 0.f; d1r = -1.f; d1i = 0.f;
+            } else if (kind == OP_NEGHI) {
+                for (int j = 0; j < nv; j++) {
+                    if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
+                    o << R(j) << " ^= 0x8000000000000000ull; " << I(j) << " ^= 0x8000000000000000ull;\n";
                 }
+            } else if (kind == OP_DREG) {
+                const float d0r = m[0], d0i = m[1], d1r = m[6], d1i = m[7];
                 o << "const v2 Rr = vpack(" << flit(d0r) << ", " << flit(d1r) << "), Ii = vpack("
                   << flit(d0i) << ", " << flit(d1i) << "), In = vpack(" << flit(-d0i) << ", "
                   << flit(-d1i) << ");\n";
@@ -245,12 +266,7 @@ struct Gen {
                 consts(nm, v, 6);
                 break;
             }
-            case OP_NEGHI: {
-                const char* nm[] = {"n1"};
-                const float v[] = {-1.f};
-                consts(nm, v, 1);
-                break;
-            }
+            case OP_NEGHI: break;
             default: break;
         }
         const bool d0one = (op.flags & OPF_D0_ONE) != 0;
@@ -313,10 +329,13 @@ struct Gen {
                         assign(I(j), "vfma(fi, lr, vmul(fr, li))", "li", k0, k1);
                     }
                     break;
-                case OP_NEGHI:
-                    assign(R(h), "vmul(n1, hr)", "hr", k0, k1);
-                    assign(I(h), "vmul(n1, hi)", "hi", k0, k1);
+                case OP_NEGHI: {
+                    // sign flips as bit XORs: they run on the ALU pipe, not the FMA pipe
+                    const char* mask = k0 && k1 ? "0x8000000080000000ull"
+                                                : (k0 ? "0x80000000ull" : "0x8000000000000000ull");
+                    o << R(h) << " = hr ^ " << mask << "; " << I(h) << " = hi ^ " << mask << ";\n";
                     break;
+                }
                 default: break;
             }
             o << "}\n";
@@ -439,9 +458,19 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem) {
                 o << "{ const ulonglong2 q = ((const ulonglong2*)buf)[(sb" << p << " ^ " << c
                   << "u) >> 1]; r" << j << " = q.x; i" << j << " = q.y; }\n";
         }
-        o << "float2 acc = make_float2(1.f, 0.f);\n(void)acc;\n";
+        o << "float2 acc = make_float2(1.f, 0.f);\n(void)acc;\nbool negf = false;\n(void)negf;\n";
         bool uses_acc = false;
+        g.uses_neg = false;
         for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) g.op(prog.ops[oi], uses_acc);
+        if (g.uses_neg && uses_acc) {
+            o << "if (negf) { acc.x = -acc.x; acc.y = -acc.y; }\n";
+        } else if (g.uses_neg) {
+            // a sign: flip the sign bits (ALU pipe) of every amplitude
+            o << "if (negf) {\n";
+            for (int j = 0; j < NV; j++)
+                o << "r" << j << " ^= 0x8000000080000000ull; i" << j << " ^= 0x8000000080000000ull;\n";
+            o << "}\n";
+        }
         if (uses_acc || P.scale != 1.f) {
             o << "{ float2 f = acc;\n";
             if (P.scale != 1.f) o << "f.x *= " << flit(P.scale) << "; f.y *= " << flit(P.scale) << ";\n";
