@@ -1,22 +1,370 @@
-// Tensor-core TransMM contraction (tcgen05): split-BF16 x3 and TF32.
+// Tensor-core TransMM contraction for sm_103a (tcgen05 + TMEM).
+//
+// A group of m = 6 qubits fused into a 64x64 complex unitary U is applied to
+// every tile of 2^13 amplitudes gathered in place (rows = the group's qubits,
+// columns = 128 other qubits), as the real-form GEMM
+//
+//     [Cr; Ci] (128 x 128) = [[Ur, -Ui], [Ui, Ur]] (128 x 128) . [Br; Bi] (128 x 128)
+//
+// on the 5th-generation tensor cores: operands in shared memory (K-major,
+// canonical 8x16-byte core matrices, no swizzle), the FP32 accumulator in
+// tensor memory, MMAs issued by one thread and completed through an mbarrier.
+//   HQ_MM_BF16X3: U and B split into hi + lo BF16; D = Uhi.Bhi + Uhi.Blo +
+//                 Ulo.Bhi (the lo.lo product, ~2^-16 relative, is dropped).
+//   HQ_MM_TF32:   one product with TF32-rounded operands.
+// Replaces the reference's cuTT transpose + cublasZgemm/Cgemm
+// (src/executor.cpp:533-551): the transpose is folded into the tile gather.
+//
+// Every wait is bounded: on expiry the kernel records an error word (read by
+// the host as HQ_ERR_TIMEOUT), frees its tensor memory and returns.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "common.h"
+#include "tile_io.cuh"
 #include "transmm.h"
 
 namespace hq {
 
+namespace {
+
+constexpr int TC_THREADS = 128;
+constexpr int TC_TILE_BITS = 13;
+constexpr int TC_ROWS = 64;      // 2^m, m = 6
+constexpr int TC_COLS = 128;     // 2^(13 - m)
+constexpr uint32_t SM_T = 0;           // tile, float2[8192]
+constexpr uint32_t SM_A = 65536;       // A operand, 64 KB
+constexpr uint32_t SM_B = 131072;      // B operand, 64 KB
+constexpr uint32_t SM_MISC = 196608;   // mbarrier, TMEM slot, row/column slot tables
+constexpr uint32_t SM_TOTAL = SM_MISC + 1024;
+constexpr uint32_t TMEM_COLS = 128;
+constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier polls (with nanosleep)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: start, leading (K) and stride (M/N)
+// byte offsets >> 4, version 1 (bits 46-47), no swizzle.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) |
+           ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor: F32 accumulator, A/B format, K-major A and B, N, M.
+__host__ __device__ constexpr uint32_t make_idesc(uint32_t ab_format, uint32_t M, uint32_t N) {
+    return (1u << 4) | (ab_format << 7) | (ab_format << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t addr, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+    for (uint32_t i = 0; i < kWaitLimit; i++) {
+        if (mbar_test(addr, parity)) return true;
+        __nanosleep(32);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+        "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+        "%28, %29, %30, %31}, [%32];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+          "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+          "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+          "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ float to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// Byte offset of element (row, k) in a K-major no-swizzle operand with
+// `kdim` K-elements of `esize` bytes per row.
+__host__ __device__ __forceinline__ uint32_t kmajor_off(uint32_t row, uint32_t k, uint32_t kdim,
+                                                        uint32_t esize) {
+    const uint32_t per_core = 16 / esize;  // K-elements per 16-byte core row
+    const uint32_t sbo = (kdim / per_core) * 128;
+    return (row / 8) * sbo + (k / per_core) * 128 + (row % 8) * 16 + (k % per_core) * esize;
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunch p) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    float2* T = reinterpret_cast<float2*>(smem + SM_T);
+    uint32_t* rowslot = reinterpret_cast<uint32_t*>(smem + SM_MISC + 64);
+    uint32_t* colslot = rowslot + TC_ROWS;
+    const uint32_t sb = smem_u32(smem);
+    const uint32_t s_mbar = sb + SM_MISC;
+    const uint32_t s_tslot = sb + SM_MISC + 8;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    float2* __restrict__ state = reinterpret_cast<float2*>(p.state);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_tslot),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    for (int r = t; r < TC_ROWS; r += TC_THREADS) {
+        uint32_t x = 0;
+        for (int b = 0; b < 6; b++)
+            if ((r >> b) & 1) x |= 1u << p.row_local[b];
+        rowslot[r] = tile_swz(x);
+    }
+    for (int c = t; c < TC_COLS; c += TC_THREADS) {
+        uint32_t x = 0;
+        for (int b = 0; b < 7; b++)
+            if ((c >> b) & 1) x |= 1u << p.col_local[b];
+        colslot[c] = tile_swz(x);
+    }
+    // the group's A operand (prepared once per circuit), 64 KB
+    const char* asrc = reinterpret_cast<const char*>(p.umat);
+    for (int i = t; i < 4096; i += TC_THREADS) cp_async16(sb + SM_A + i * 16u, asrc + i * 16);
+    cp_async_commit();
+    cp_async_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + SM_MISC + 8);
+
+    const uint64_t toff = local_to_phys(uint32_t(t) << 1, TC_TILE_BITS, p.tile_phys);
+    const uint32_t tsl = tile_swz(uint32_t(t) << 1);
+    constexpr uint32_t esize = PREC == HQ_MM_TF32 ? 4 : 2;
+    constexpr uint32_t kstep_bytes = 256;  // 16 bf16 or 8 tf32 K-elements = two core matrices
+    constexpr uint32_t sbo = (128 / (16 / esize)) * 128;
+    constexpr uint32_t idesc = make_idesc(PREC == HQ_MM_TF32 ? 2u : 1u, 128, 128);
+    const int nsteps = PREC == HQ_MM_TF32 ? 16 : 8;
+
+    int it = 0;
+    for (uint64_t u = blockIdx.x; u < p.ntiles; u += gridDim.x, it++) {
+        const uint64_t base = tile_base(u, p.nruns, p.run_src, p.run_dst, p.run_len);
+        const float2* gsrc = state + base + toff;
+#pragma unroll 8
+        for (int m = 0; m < 32; m++)
+            cp_async16(sb + SM_T + (tsl ^ p.piece_slot128[m]) * 8u, gsrc + p.piece_off128[m]);
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncthreads();
+
+        // B operand: column n = t; K index k = component * 64 + row
+        {
+            const uint32_t cs = colslot[t];
+            for (int rb = 0; rb < 8; rb++) {
+                float re[8], im[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const float2 a = T[rowslot[rb * 8 + q] ^ cs];
+                    re[q] = a.x;
+                    im[q] = a.y;
+                }
+                if (PREC == HQ_MM_TF32) {
+#pragma unroll
+                    for (int half = 0; half < 2; half++) {
+                        const uint32_t ore = kmajor_off(t, rb * 8 + half * 4, 128, 4);
+                        const uint32_t oim = kmajor_off(t, 64 + rb * 8 + half * 4, 128, 4);
+                        *reinterpret_cast<float4*>(smem + SM_B + ore) =
+                            make_float4(to_tf32(re[4 * half]), to_tf32(re[4 * half + 1]),
+                                        to_tf32(re[4 * half + 2]), to_tf32(re[4 * half + 3]));
+                        *reinterpret_cast<float4*>(smem + SM_B + oim) =
+                            make_float4(to_tf32(im[4 * half]), to_tf32(im[4 * half + 1]),
+                                        to_tf32(im[4 * half + 2]), to_tf32(im[4 * half + 3]));
+                    }
+                } else {
+                    uint32_t hre[4], lre[4], him[4], lim[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const __nv_bfloat16 h0 = __float2bfloat16_rn(re[2 * q]);
+                        const __nv_bfloat16 h1 = __float2bfloat16_rn(re[2 * q + 1]);
+                        const __nv_bfloat16 l0 = __float2bfloat16_rn(re[2 * q] - __bfloat162float(h0));
+                        const __nv_bfloat16 l1 =
+                            __float2bfloat16_rn(re[2 * q + 1] - __bfloat162float(h1));
+                        hre[q] = pack_bf16(h0, h1);
+                        lre[q] = pack_bf16(l0, l1);
+                        const __nv_bfloat16 g0 = __float2bfloat16_rn(im[2 * q]);
+                        const __nv_bfloat16 g1 = __float2bfloat16_rn(im[2 * q + 1]);
+                        const __nv_bfloat16 k0 = __float2bfloat16_rn(im[2 * q] - __bfloat162float(g0));
+                        const __nv_bfloat16 k1 =
+                            __float2bfloat16_rn(im[2 * q + 1] - __bfloat162float(g1));
+                        him[q] = pack_bf16(g0, g1);
+                        lim[q] = pack_bf16(k0, k1);
+                    }
+                    const uint32_t ore = kmajor_off(t, rb * 8, 128, 2);
+                    const uint32_t oim = kmajor_off(t, 64 + rb * 8, 128, 2);
+                    *reinterpret_cast<uint4*>(smem + SM_B + ore) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+                    *reinterpret_cast<uint4*>(smem + SM_B + oim) = make_uint4(him[0], him[1], him[2], him[3]);
+                    *reinterpret_cast<uint4*>(smem + SM_B + 32768 + ore) =
+                        make_uint4(lre[0], lre[1], lre[2], lre[3]);
+                    *reinterpret_cast<uint4*>(smem + SM_B + 32768 + oim) =
+                        make_uint4(lim[0], lim[1], lim[2], lim[3]);
+                }
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+
+        if (t == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            if (PREC == HQ_MM_TF32) {
+                for (int kk = 0; kk < nsteps; kk++)
+                    mma_tf32(tmem, make_desc(sb + SM_A + kk * kstep_bytes, 128, sbo),
+                             make_desc(sb + SM_B + kk * kstep_bytes, 128, sbo), idesc, kk > 0);
+            } else {
+                for (int kk = 0; kk < nsteps; kk++)  // hi . hi
+                    mma_f16(tmem, make_desc(sb + SM_A + kk * kstep_bytes, 128, sbo),
+                            make_desc(sb + SM_B + kk * kstep_bytes, 128, sbo), idesc, kk > 0);
+                for (int kk = 0; kk < nsteps; kk++)  // hi . lo
+                    mma_f16(tmem, make_desc(sb + SM_A + kk * kstep_bytes, 128, sbo),
+                            make_desc(sb + SM_B + 32768 + kk * kstep_bytes, 128, sbo), idesc, 1);
+                for (int kk = 0; kk < nsteps; kk++)  // lo . hi
+                    mma_f16(tmem, make_desc(sb + SM_A + 32768 + kk * kstep_bytes, 128, sbo),
+                            make_desc(sb + SM_B + kk * kstep_bytes, 128, sbo), idesc, 1);
+            }
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                    s_mbar)
+                : "memory");
+        }
+        const bool ok = mbar_wait(s_mbar, uint32_t(it & 1));
+        if (__syncthreads_or(!ok)) {
+            if (t == 0 && p.err) {
+                atomicCAS(p.err, 0, 1);
+                p.err[1] = 7;  // site: TransMM accumulator wait
+                p.err[2] = (int)(u & 0x7fffffff);
+            }
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+        // D row i (TMEM lane i): i < 64 -> real part of row i, else imaginary of row i-64
+        {
+            const int i = 32 * warp + lane;
+            const uint32_t rs = rowslot[i & 63];
+            float* Tf = reinterpret_cast<float*>(T);
+            const uint32_t comp = uint32_t(i >> 6);
+#pragma unroll 1
+            for (int c = 0; c < 4; c++) {
+                uint32_t v[32];
+                tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 32 * c, v);
+#pragma unroll
+                for (int q = 0; q < 32; q++)
+                    Tf[2 * (rs ^ colslot[32 * c + q]) + comp] = __uint_as_float(v[q]);
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+
+        float2* gdst = state + base + toff;
+#pragma unroll 8
+        for (int m = 0; m < 32; m++)
+            *reinterpret_cast<float4*>(gdst + p.piece_off128[m]) =
+                reinterpret_cast<const float4*>(T)[(tsl ^ p.piece_slot128[m]) >> 1];
+        __syncthreads();
+    }
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
+// A operand from the FP64 unitary U (64 x 64, column-major): the real form
+// [[Ur, -Ui], [Ui, Ur]] (128 x 128) in the K-major core layout.
+__global__ void k_u_to_tc(const double2* __restrict__ U, unsigned char* __restrict__ out, int prec) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 128 * 128) return;
+    const int i = idx / 128, k = idx % 128;
+    const int r = i & 63, c = k & 63;
+    const double2 u = U[(size_t)c * 64 + r];
+    double v;
+    if (i < 64)
+        v = k < 64 ? u.x : -u.y;
+    else
+        v = k < 64 ? u.y : u.x;
+    if (prec == HQ_MM_TF32) {
+        *reinterpret_cast<float*>(out + kmajor_off(i, k, 128, 4)) = to_tf32((float)v);
+    } else {
+        const __nv_bfloat16 hi = __float2bfloat16_rn((float)v);
+        const __nv_bfloat16 lo = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
+        *reinterpret_cast<__nv_bfloat16*>(out + kmajor_off(i, k, 128, 2)) = hi;
+        *reinterpret_cast<__nv_bfloat16*>(out + 32768 + kmajor_off(i, k, 128, 2)) = lo;
+    }
+}
+
+}  // namespace
+
 size_t transmm_tc_operand_bytes(int m, int precision) {
     (void)precision;
-    return size_t(16) << (2 * m);
+    HQ_REQUIRE(m == 6, HQ_ERR_UNSUPPORTED, "tensor-core TransMM runs 6-qubit groups (got %d)", m);
+    return 65536;
 }
 
-void launch_u_to_tc_operand(int, int, const double*, void*, cudaStream_t) {
-    fail(HQ_ERR_UNSUPPORTED, "tensor-core TransMM not available in this build");
+void launch_u_to_tc_operand(int m, int precision, const double* d_u, void* d_out, cudaStream_t st) {
+    HQ_REQUIRE(m == 6, HQ_ERR_UNSUPPORTED, "tensor-core TransMM runs 6-qubit groups (got %d)", m);
+    k_u_to_tc<<<64, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
+    HQ_CHECK_CUDA(cudaGetLastError());
 }
 
-void launch_transmm_tc(const TransmmLaunch&, cudaStream_t) {
-    fail(HQ_ERR_UNSUPPORTED, "tensor-core TransMM not available in this build");
+template <int PREC>
+static void launch_prec(const TransmmLaunch& p, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        HQ_CHECK_CUDA(cudaFuncSetAttribute(k_transmm_tc<PREC>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM_TOTAL));
+        attr = true;
+    }
+    const uint64_t slots = uint64_t(ctx().sm_count);
+    const unsigned grid = (unsigned)(p.ntiles < slots ? p.ntiles : slots);
+    k_transmm_tc<PREC><<<grid, TC_THREADS, SM_TOTAL, st>>>(p);
+    HQ_CHECK_CUDA(cudaGetLastError());
+}
+
+void launch_transmm_tc(const TransmmLaunch& p, cudaStream_t st) {
+    HQ_REQUIRE(p.m == 6 && p.k == TC_TILE_BITS, HQ_ERR_UNSUPPORTED,
+               "tensor-core TransMM runs 6-qubit groups on 13-qubit tiles");
+    if (p.precision == HQ_MM_TF32)
+        launch_prec<HQ_MM_TF32>(p, st);
+    else
+        launch_prec<HQ_MM_BF16X3>(p, st);
 }
 
 }  // namespace hq

@@ -183,8 +183,9 @@ void launch_transmm_simt(const TransmmLaunch& p, cudaStream_t st) {
 
 // ---- host glue ---------------------------------------------------------------------
 
+// group widths each contraction runs (narrower groups are padded with idle qubits)
 static int min_mm_qubits(int precision) { return precision == HQ_MM_FP32 ? 4 : 6; }
-static int max_mm_qubits(int precision) { return precision == HQ_MM_FP32 ? 7 : 7; }
+static int max_mm_qubits(int precision) { return precision == HQ_MM_FP32 ? 7 : 6; }
 
 // Rows = the group's qubits padded up to the kernel's minimum with the lowest
 // free physical qubits; tile = rows + lowest non-row qubits up to 13 bits.
@@ -269,6 +270,14 @@ static TransmmLaunch make_launch(int n, int m, uint64_t rows, uint64_t tile, int
             if ((local >> j) & 1) off |= uint64_t(1) << p.tile_phys[j];
         p.piece_off[mm] = off;
         p.piece_slot[mm] = tile_swz(local);
+    }
+    for (int mm = 0; mm < 32; mm++) {
+        const uint32_t local = uint32_t(2 * mm * 128);
+        uint64_t off = 0;
+        for (int j = 0; j < kSimtK; j++)
+            if ((local >> j) & 1) off |= uint64_t(1) << p.tile_phys[j];
+        p.piece_off128[mm] = off;
+        p.piece_slot128[mm] = tile_swz(local);
     }
     return p;
 }

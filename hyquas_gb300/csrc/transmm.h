@@ -29,8 +29,10 @@ struct TransmmLaunch {
     uint8_t tile_phys[16];    // physical bit of local tile bit j (ascending)
     uint8_t row_local[8];     // local tile bit of row bit r
     uint8_t col_local[16];    // local tile bit of column bit c
-    uint64_t piece_off[32];
+    uint64_t piece_off[32];       // 512-thread piece tables (SIMT kernel)
     uint32_t piece_slot[32];
+    uint64_t piece_off128[32];    // 128-thread piece tables (tensor-core kernel)
+    uint32_t piece_slot128[32];
 };
 
 void transmm_prepare(int n, const GroupPlan& gp, DeviceGroup& dg, const CompileConfig& cfg,

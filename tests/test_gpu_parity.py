@@ -112,7 +112,8 @@ def test_oshm_scattered_tile(hq, oracle, seed):
 
 @pytest.mark.parametrize("backend,tile,prec", [
     ("oshm", 13, "bf16x3"), ("oshm", 10, "bf16x3"), ("oshm", 8, "bf16x3"),
-    ("transmm", 0, "fp32"), ("hybrid", 13, "fp32"), ("plain", 0, "fp32")])
+    ("transmm", 0, "fp32"), ("transmm", 0, "bf16x3"), ("hybrid", 13, "fp32"),
+    ("hybrid", 13, "bf16x3"), ("plain", 0, "fp32")])
 @pytest.mark.parametrize("n", [16, 20])
 def test_compiled_random_circuits(hq, oracle, backend, tile, prec, n):
     desc = random_circuit(600 + n, n, 400)
@@ -187,8 +188,13 @@ def test_group_unitary_fp64_matches_oracle(hq, oracle):
     np.testing.assert_allclose(U, oracle.group_unitary(list(range(7)), desc), atol=1e-12)
 
 
-@pytest.mark.parametrize("prec", ["fp32"])
-@pytest.mark.parametrize("m", [4, 5, 6, 7])
+# TransMM tolerances per arithmetic: BF16x3 and FP32 meet the 1e-5 bar; TF32
+# (10-bit mantissa) is the low-precision comparison variant.
+MM_TOL = {"fp32": (TOL, FID), "bf16x3": (TOL, FID), "tf32": (5e-5, 1e-5)}
+
+
+@pytest.mark.parametrize("prec,m", [("fp32", 4), ("fp32", 5), ("fp32", 6), ("fp32", 7),
+                                    ("bf16x3", 4), ("bf16x3", 6), ("tf32", 6)])
 def test_transmm_single_group(hq, oracle, prec, m):
     n = 17
     rng = W.SplitMix64(900 + m)
@@ -198,7 +204,27 @@ def test_transmm_single_group(hq, oracle, prec, m):
     s = hq.State(n, zero=False)
     s.load(psi)
     s.apply_transmm_group(W.to_gates(desc), sum(1 << q for q in qubits), prec)
-    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+    tol, fid = MM_TOL[prec]
+    c = oracle.compare(oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+    assert c["max_abs_err"] <= tol and c["one_minus_fidelity"] <= fid, c
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32", "fp32"])
+def test_transmm_qft_precision_sweep(hq, oracle, prec):
+    """Config-3 shape at a size the oracle finishes: QFT on a random state,
+    TransMM groups only, per arithmetic."""
+    n = 18
+    desc = W.qft(n)
+    psi = W.random_state(31, n)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile(backend="transmm", precision=prec, mm_qubits=6)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    c.run_on(s)
+    tol, fid = MM_TOL[prec]
+    r = oracle.compare(oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+    assert r["max_abs_err"] <= tol and r["one_minus_fidelity"] <= fid, r
 
 
 def inverse(desc):
