@@ -412,6 +412,14 @@ using namespace hq;
     }                                             \
     return HQ_OK;
 
+// widen a row set to the contraction's minimum width with the lowest free
+// physical qubits (the fused unitary acts as identity on them)
+static uint64_t pad_rows(int n, uint64_t rows, int precision) {
+    for (int b = 0; b < n && __builtin_popcountll(rows) < min_mm_qubits(precision); b++)
+        rows |= uint64_t(1) << b;
+    return rows;
+}
+
 static uint64_t logical_to_phys_mask(const hq_state_s* s, uint64_t logical) {
     uint64_t m = 0;
     for (int q = 0; q < s->n; q++)
@@ -458,7 +466,8 @@ extern "C" hq_status hq_apply_transmm_group(hq_state s, const hq_gate* gates, in
         if (g.control2 >= 0) g.control2 = s->pos[g.control2];
         phys.push_back(g);
     }
-    const uint64_t rows = logical_to_phys_mask(s, group_mask);
+    uint64_t rows = logical_to_phys_mask(s, group_mask);
+    rows = pad_rows(s->n, rows, precision);
     const int m = __builtin_popcountll(rows);
     std::vector<ComposeGate> cg = to_compose(phys, rows);
     const size_t ub = sizeof(double) * (size_t(2) << (2 * m));
@@ -508,11 +517,45 @@ extern "C" hq_status hq_apply_unitary(hq_state s, const double* unitary, uint64_
             u[dst] = unitary[src];
             u[dst + 1] = unitary[src + 1];
         }
+    // pad to the contraction's width: U' = U on the original rows, identity on the added ones
+    const uint64_t prow = pad_rows(s->n, rows, precision);
+    const int pm = __builtin_popcountll(prow);
+    if (pm != m) {
+        std::vector<int> orig_bit;  // padded local bit -> original local bit or -1
+        for (int b = 0, j = 0; b < s->n; b++) {
+            if (!((prow >> b) & 1)) continue;
+            int o = -1;
+            if ((rows >> b) & 1) o = __builtin_popcountll(rows & ((uint64_t(1) << b) - 1));
+            orig_bit.push_back(o);
+            j++;
+        }
+        const size_t pdim = size_t(1) << pm;
+        std::vector<double> pu(2 * pdim * pdim, 0.0);
+        for (size_t c = 0; c < pdim; c++)
+            for (size_t r = 0; r < pdim; r++) {
+                size_t oc = 0, orr = 0;
+                bool same_extra = true;
+                for (int b = 0; b < pm; b++) {
+                    const int o = orig_bit[b];
+                    const size_t cb = (c >> b) & 1, rb = (r >> b) & 1;
+                    if (o < 0) {
+                        if (cb != rb) same_extra = false;
+                    } else {
+                        oc |= cb << o;
+                        orr |= rb << o;
+                    }
+                }
+                if (!same_extra) continue;
+                pu[2 * (c * pdim + r)] = u[2 * (oc * dim + orr)];
+                pu[2 * (c * pdim + r) + 1] = u[2 * (oc * dim + orr) + 1];
+            }
+        u.swap(pu);
+    }
     const size_t ub = sizeof(double) * u.size();
     double* d_u = (double*)dev_alloc(ub);
     try {
         HQ_CHECK_CUDA(cudaMemcpy(d_u, u.data(), ub, cudaMemcpyHostToDevice));
-        apply_unitary_device(s, d_u, m, rows, precision);
+        apply_unitary_device(s, d_u, pm, prow, precision);
     } catch (...) {
         dev_free(d_u, ub);
         throw;

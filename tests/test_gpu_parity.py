@@ -209,6 +209,20 @@ def test_transmm_single_group(hq, oracle, prec, m):
     assert c["max_abs_err"] <= tol and c["one_minus_fidelity"] <= fid, c
 
 
+@pytest.mark.parametrize("prec", ["bf16x3", "fp32"])
+def test_apply_caller_unitary_narrow_group(hq, oracle, prec):
+    """A 3-qubit unitary given by the caller, widened to the contraction width."""
+    n = 15
+    qubits = [2, 7, 11]
+    desc = random_circuit(950, n, 40, qubits=qubits)
+    U = oracle.group_unitary(qubits, desc)
+    psi = W.random_state(19, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    s.apply_unitary(U, sum(1 << q for q in qubits), prec)
+    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+
+
 @pytest.mark.parametrize("prec", ["bf16x3", "tf32", "fp32"])
 def test_transmm_qft_precision_sweep(hq, oracle, prec):
     """Config-3 shape at a size the oracle finishes: QFT on a random state,
