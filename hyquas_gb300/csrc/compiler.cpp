@@ -575,38 +575,39 @@ OshmLaunch make_oshm_launch(const OshmProgram& prog, void* state, const OshmPhas
 }
 
 // ---- GB300 cost model --------------------------------------------------------
-// Seconds per pass, refitted constants (see costmodel section of the design
-// notes): a pass moves 16 * 2^n bytes; OShareMem compute is ~4 instructions
-// per amplitude per non-diagonal gate on 152 SMs x 128 lanes; TransMM runs
-// 3 BF16 products on the tensor pipe.
-static const double kHbmBytesPerSec = 5.6e12;      // sustained pass bandwidth
-static const double kSimtInstrPerSec = 3.3e13;     // issued thread-instructions
-static const double kTensorFlopsPerSec = 1.5e15;   // BF16 dense, sustained
+// Seconds per pass over 2^n amplitudes, fitted to CUDA-event times of the
+// kernels on a GB300 (30-qubit grid circuit, 28-qubit QFT; see the design
+// notes): a pass costs its HBM floor (16 B per amplitude at the measured copy
+// bandwidth) plus, for OShareMem, FP32 work per gate.  Replaces the
+// reference's V100 tables (src/evaluator.h:18-127, src/evaluator.cpp:111-229).
+static const double kPassFloor = 2.4e-12;       // s per amplitude: 16 B at 6.7 TB/s
+static const double kOshmGate = 6.6e-14;        // s per amplitude per non-diagonal gate
+static const double kOshmDiag = 0.3 * 6.6e-14;  // uncontrolled diagonal gate
+static const double kOshmCtrlDiag = 1.4 * 6.6e-14;  // controlled diagonal gate
+static const double kMmBf16x3 = 7.8e-12;        // s per amplitude per 6-qubit TransMM pass
+static const double kMmTf32 = 6.6e-12;
+static const double kMmFp32 = 1.5e-11;
 static const double kLaunchSec = 4e-6;
 
 double cost_oshm(int n, int nphases, const std::vector<hq_gate>& gates, int k) {
     (void)k;
+    (void)nphases;
     const double amps = double(uint64_t(1) << n);
-    double instr = 6.0;  // staging
-    for (const auto& g : gates) instr += matrix_is_diagonal(g) ? 1.0 : (is_x_like(g) ? 1.5 : 4.5);
-    instr += 4.0 * (nphases > 0 ? nphases : 1 + (double)gates.size() / 12.0);
-    const double t_mem = 16.0 * amps / kHbmBytesPerSec;
-    const double t_cmp = instr * amps / kSimtInstrPerSec;
-    return std::max(t_mem, t_cmp) + kLaunchSec;
+    double w = 0;
+    for (const auto& g : gates) {
+        if (!matrix_is_diagonal(g))
+            w += kOshmGate;
+        else
+            w += g.control >= 0 ? kOshmCtrlDiag : kOshmDiag;
+    }
+    return amps * (kPassFloor + w) + kLaunchSec;
 }
 
 double cost_transmm(int n, int m, int precision) {
     const double amps = double(uint64_t(1) << n);
-    const double t_mem = 16.0 * amps / kHbmBytesPerSec;
-    const double flops = 8.0 * amps * double(uint64_t(1) << m);
-    double t_cmp;
-    if (precision == HQ_MM_FP32)
-        t_cmp = flops / 6.0e13;
-    else if (precision == HQ_MM_TF32)
-        t_cmp = flops / (kTensorFlopsPerSec / 2);
-    else
-        t_cmp = 3.0 * flops / kTensorFlopsPerSec;
-    return std::max(t_mem, t_cmp) + kLaunchSec;
+    double per = precision == HQ_MM_FP32 ? kMmFp32 : (precision == HQ_MM_TF32 ? kMmTf32 : kMmBf16x3);
+    if (precision == HQ_MM_FP32 && m > 6) per *= double(1 << (m - 6));  // SIMT flops grow with 2^m
+    return amps * per + kLaunchSec;
 }
 
 }  // namespace hq
