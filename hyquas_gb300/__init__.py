@@ -104,6 +104,14 @@ def _load():
         "hq_apply_transmm_group": [P, P, I32, U64, I32],
         "hq_apply_unitary": [P, P, U64, I32],
         "hq_group_unitary": [P, I32, U64, P],
+        "hq_batch_create": [C.POINTER(P)],
+        "hq_batch_destroy": [P],
+        "hq_batch_add": [P, P, P, C.POINTER(I32)],
+        "hq_batch_compile": [P, C.POINTER(hq_compile_options)],
+        "hq_batch_run": [P, I32, C.POINTER(D)],
+        "hq_batch_enqueue": [P, I32],
+        "hq_batch_capture_graph": [P, I32],
+        "hq_batch_info": [P, C.POINTER(I32), C.POINTER(I64), C.POINTER(I64), C.POINTER(U64), P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -504,5 +512,66 @@ class Circuit:
             pass
 
 
-__all__ = ["Circuit", "Gate", "State", "ResultItem", "HQError", "init", "device_info",
+class Batch:
+    """Many circuits (uneven qubit counts) in one persistent launch.
+
+    add(circuit, state) pairs a circuit with the state it runs on; compile()
+    plans every circuit as OShareMem groups (tile width per circuit from the
+    cost model unless tile_qubits is given); run() executes all of them."""
+
+    def __init__(self):
+        self._h = C.c_void_p()
+        check(lib.hq_batch_create(C.byref(self._h)))
+        self._keep: list = []  # circuits and states must outlive the batch's runs
+
+    @property
+    def handle(self):
+        return self._h
+
+    def add(self, circuit: "Circuit", state: State) -> int:
+        idx = C.c_int32()
+        check(lib.hq_batch_add(self._h, circuit.handle, state.handle, C.byref(idx)))
+        self._keep.append((circuit, state))
+        return idx.value
+
+    def compile(self, tile_qubits: int = 0, coalesce: int = 0):
+        o = hq_compile_options()
+        check(lib.hq_compile_options_default(C.byref(o)))
+        o.tile_qubits = tile_qubits
+        o.coalesce = coalesce
+        check(lib.hq_batch_compile(self._h, C.byref(o)))
+
+    def run(self, zero_init: bool = True) -> float:
+        """Run every circuit once; returns device microseconds."""
+        us = C.c_double()
+        check(lib.hq_batch_run(self._h, 1 if zero_init else 0, C.byref(us)))
+        return us.value
+
+    def enqueue(self, zero_init: bool = True):
+        check(lib.hq_batch_enqueue(self._h, 1 if zero_init else 0))
+
+    def capture_graph(self, zero_init: bool = True):
+        check(lib.hq_batch_capture_graph(self._h, 1 if zero_init else 0))
+
+    def info(self) -> dict:
+        nc, ng, ni, pb = C.c_int32(), C.c_int64(), C.c_int64(), C.c_uint64()
+        check(lib.hq_batch_info(self._h, C.byref(nc), C.byref(ng), C.byref(ni), C.byref(pb), None))
+        tiles = (C.c_int32 * max(1, nc.value))()
+        check(lib.hq_batch_info(self._h, None, None, None, None, tiles))
+        return {"circuits": nc.value, "groups": ng.value, "items": ni.value,
+                "pass_bytes": pb.value, "tile_qubits": list(tiles[: nc.value])}
+
+    def free(self):
+        if self._h:
+            lib.hq_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+__all__ = ["Circuit", "Batch", "Gate", "State", "ResultItem", "HQError", "init", "device_info",
            "group_unitary", "set_hbm_budget", "hbm_in_use", "lib", "LIB_PATH"]

@@ -1,0 +1,294 @@
+// Batched execution: many circuits, one persistent launch (k_oshm_batch).
+//
+// The reference simulates one circuit per process (src/circuit.cpp:16-71,
+// src/main.cpp:12-230); it has no batching.  Here every circuit of a batch is
+// partitioned into OShareMem groups with the same grouping and lowering as a
+// single compiled circuit (compiler.cpp), the group programs of all circuits
+// are concatenated into one device program, and a work queue of
+// (circuit, group, tile range) items is built group level by group level.
+// Persistent blocks take items in queue order; an item of group g waits
+// (bounded) until every tile of groups < g of its circuit is written.
+#include <algorithm>
+#include <cstring>
+
+#include "batch.h"
+#include "common.h"
+#include "gates.h"
+
+namespace hq {
+
+namespace {
+
+// Estimated device seconds of one circuit planned with tile width k: the
+// refitted per-pass cost of every group plus a per-item dispatch overhead
+// spread over the resident blocks.
+double batch_cost(const Partition& part, const std::vector<hq_gate>& gates, int n, int k,
+                  int slots) {
+    const double kItemSec = 1.5e-6;
+    double t = 0;
+    for (const GroupPlan& gp : part.groups) {
+        std::vector<hq_gate> gs;
+        for (int x : gp.gates) gs.push_back(gates[x]);
+        t += cost_oshm(n, 0, gs, k) - 4e-6;  // no launch per group
+    }
+    const double items = double(part.groups.size()) * double(uint64_t(1) << (n - k));
+    return t + items * kItemSec / std::max(1, slots);
+}
+
+uint32_t chunk_tiles(uint64_t tiles, int slots) {
+    uint64_t c = tiles / (4 * uint64_t(std::max(1, slots)));
+    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 1), 16);
+}
+
+}  // namespace
+
+void batch_release(hq_batch_s* b) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    dev_free(b->d_program, b->program_bytes);
+    b->d_program = nullptr;
+    b->program_bytes = 0;
+    b->compiled = false;
+}
+
+void batch_compile(hq_batch_s* b, const hq_compile_options* opt) {
+    ensure_init();
+    batch_release(b);
+    const int fixed_k = opt ? opt->tile_qubits : 0;
+    HQ_REQUIRE(fixed_k == 0 || (fixed_k >= kBatchMinTile && fixed_k <= kBatchTile), HQ_ERR_INVALID,
+               "batch: tile width %d outside [%d, %d]", fixed_k, kBatchMinTile, kBatchTile);
+    const int slots = oshm_batch_slots();
+    b->slots = slots;
+
+    std::vector<OshmProgram> progs;
+    std::vector<uint32_t> prog_circuit;
+    b->num_groups = 0;
+    b->pass_bytes = 0;
+    for (BatchEntry& e : b->entries) {
+        const int n = e.n;
+        std::vector<int> perm;
+        e.folded = fold_swaps(e.gates, n, perm);
+        e.swap_perm = perm;
+        e.group0 = (uint32_t)progs.size();
+        e.ngroups = 0;
+        e.k = 0;
+        if (n < kBatchMinTile || e.folded.empty()) continue;  // gate by gate / init only
+        std::vector<int> id(n);
+        for (int q = 0; q < n; q++) id[q] = q;
+        CompileConfig cfg;
+        cfg.backend = HQ_BACKEND_OSHM;
+        cfg.coalesce = opt && opt->coalesce > 0 ? opt->coalesce : 3;
+        Partition best;
+        double best_cost = 1e300;
+        const int kmax = std::min(n, kBatchTile);
+        const int kmin = fixed_k ? std::min(fixed_k, kmax) : kBatchMinTile;
+        for (int k = fixed_k ? kmin : kmax; k >= kmin; k--) {
+            cfg.tile = k;
+            cfg.coalesce = std::min(cfg.coalesce, k);
+            Partition part = partition(n, e.folded, id, cfg);
+            const double c = batch_cost(part, e.folded, n, k, slots);
+            if (c < best_cost) {
+                best_cost = c;
+                best = std::move(part);
+                e.k = k;
+            }
+        }
+        for (const GroupPlan& gp : best.groups) {
+            std::vector<hq_gate> phys;
+            for (int x : gp.gates) phys.push_back(e.folded[x]);
+            OshmProgram prog = plan_oshm(n, phys, oshm_tile_mask(gp, n));
+            HQ_REQUIRE(prog.k == e.k && prog.r == 5, HQ_ERR_UNSUPPORTED,
+                       "batch: group planned with tile %d/%d registers", prog.k, prog.r);
+            progs.push_back(std::move(prog));
+            prog_circuit.push_back(uint32_t(&e - b->entries.data()));
+            e.ngroups++;
+        }
+        b->num_groups += e.ngroups;
+        b->pass_bytes += uint64_t(e.ngroups) * 16ull * (uint64_t(1) << n);
+    }
+
+    // one device program: groups | items | phases | ops | counters
+    std::vector<OshmPhase> phases;
+    std::vector<OshmOp> ops;
+    std::vector<size_t> phase_off(progs.size());
+    for (size_t i = 0; i < progs.size(); i++) {
+        phase_off[i] = phases.size();
+        const uint32_t o = (uint32_t)ops.size();
+        for (OshmPhase ph : progs[i].phases) {
+            ph.op_begin += o;
+            ph.op_end += o;
+            phases.push_back(ph);
+        }
+        ops.insert(ops.end(), progs[i].ops.begin(), progs[i].ops.end());
+    }
+    std::vector<BatchItem> items;
+    uint32_t levels = 0;
+    for (const BatchEntry& e : b->entries) levels = std::max(levels, e.ngroups);
+    std::vector<uint32_t> order(b->entries.size());
+    for (uint32_t i = 0; i < order.size(); i++) order[i] = i;
+    // deepest circuits first inside a level, so their chains start early
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        const BatchEntry &a = b->entries[x], &c = b->entries[y];
+        if (a.ngroups != c.ngroups) return a.ngroups > c.ngroups;
+        return a.n > c.n;
+    });
+    for (uint32_t g = 0; g < levels; g++) {
+        for (uint32_t ci : order) {
+            const BatchEntry& e = b->entries[ci];
+            if (g >= e.ngroups) continue;
+            const uint64_t tiles = uint64_t(1) << (e.n - e.k);
+            HQ_REQUIRE(tiles * e.ngroups < (uint64_t(1) << 32), HQ_ERR_UNSUPPORTED,
+                       "batch: circuit %u has too many tiles for the 32-bit item counters", ci);
+            const uint32_t ch = chunk_tiles(tiles, slots);
+            for (uint64_t u = 0; u < tiles; u += ch) {
+                BatchItem it;
+                it.group = e.group0 + g;
+                it.circuit = ci;
+                it.tile0 = (uint32_t)u;
+                it.count = (uint32_t)std::min<uint64_t>(ch, tiles - u);
+                it.need = (uint32_t)(g * tiles);
+                it.flags = g == 0 ? ITEM_FIRST : 0;
+                items.push_back(it);
+            }
+        }
+    }
+    b->num_items = items.size();
+    HQ_REQUIRE(items.size() < (uint64_t(1) << 32) - 1, HQ_ERR_UNSUPPORTED, "batch: too many items");
+
+    auto up16 = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t groups_b = up16(sizeof(OshmLaunch) * std::max<size_t>(progs.size(), 1));
+    const size_t items_b = up16(sizeof(BatchItem) * std::max<size_t>(items.size(), 1));
+    const size_t phases_b = up16(sizeof(OshmPhase) * std::max<size_t>(phases.size(), 1));
+    const size_t ops_b = up16(sizeof(OshmOp) * std::max<size_t>(ops.size(), 1));
+    const size_t ctr_b = up16(sizeof(uint32_t) * (1 + b->entries.size()));
+    b->program_bytes = groups_b + items_b + phases_b + ops_b + ctr_b;
+    b->d_program = (char*)dev_alloc(b->program_bytes);
+    char* base = b->d_program;
+    OshmLaunch* d_groups = (OshmLaunch*)base;
+    BatchItem* d_items = (BatchItem*)(base + groups_b);
+    OshmPhase* d_phases = (OshmPhase*)(base + groups_b + items_b);
+    OshmOp* d_ops = (OshmOp*)(base + groups_b + items_b + phases_b);
+    b->d_counters = (uint32_t*)(base + groups_b + items_b + phases_b + ops_b);
+    b->counters_bytes = sizeof(uint32_t) * (1 + b->entries.size());
+
+    std::vector<OshmLaunch> launches;
+    for (size_t i = 0; i < progs.size(); i++) {
+        const BatchEntry& e = b->entries[prog_circuit[i]];
+        launches.push_back(make_oshm_launch(progs[i], e.s->d, d_phases + phase_off[i], d_ops,
+                                            ctx().d_error));
+    }
+    cudaStream_t st = ctx().stream;
+    auto put = [&](void* dst, const void* src, size_t bytes) {
+        if (bytes) HQ_CHECK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    };
+    put(d_groups, launches.data(), sizeof(OshmLaunch) * launches.size());
+    put(d_items, items.data(), sizeof(BatchItem) * items.size());
+    put(d_phases, phases.data(), sizeof(OshmPhase) * phases.size());
+    put(d_ops, ops.data(), sizeof(OshmOp) * ops.size());
+    HQ_CHECK_CUDA(cudaStreamSynchronize(st));
+
+    b->launch = BatchLaunch{};
+    b->launch.groups = d_groups;
+    b->launch.items = d_items;
+    b->launch.nitems = (uint32_t)items.size();
+    b->launch.head = b->d_counters;
+    b->launch.done = b->d_counters + 1;
+    b->launch.err = ctx().d_error;
+    b->grid = (int)std::min<uint64_t>(uint64_t(slots), std::max<uint64_t>(items.size(), 1));
+    b->compiled = true;
+}
+
+// Everything one run enqueues: layouts, gate-by-gate circuits, counter reset,
+// the persistent launch.
+static void batch_enqueue_work(hq_batch_s* b, bool zero_init, cudaStream_t st) {
+    for (BatchEntry& e : b->entries) {
+        if (zero_init) {
+            for (int q = 0; q < e.n; q++) e.s->pos[q] = q;  // contents are rewritten
+            if (e.ngroups == 0) launch_init_zero(e.s->d, e.n, st);
+        } else {
+            state_canonicalize(e.s);
+        }
+        if (e.ngroups == 0 && !e.folded.empty()) apply_plain(e.s, e.folded);
+    }
+    if (b->num_items) {
+        HQ_CHECK_CUDA(cudaMemsetAsync(b->d_counters, 0, b->counters_bytes, st));
+        BatchLaunch l = b->launch;
+        l.zero_init = zero_init ? 1u : 0u;
+        launch_oshm_batch(l, b->grid, b->cooperative, st);
+    }
+    for (BatchEntry& e : b->entries)
+        for (int q = 0; q < e.n; q++) e.s->pos[q] = e.swap_perm[q];
+}
+
+void batch_enqueue(hq_batch_s* b, bool zero_init) {
+    HQ_REQUIRE(b->compiled, HQ_ERR_STATE, "batch not compiled");
+    cudaStream_t st = ctx().stream;
+    if (b->graph && b->graph_zero == zero_init) {
+        for (BatchEntry& e : b->entries) {
+            if (!zero_init) state_canonicalize(e.s);
+        }
+        HQ_CHECK_CUDA(cudaGraphLaunch(b->graph, st));
+        for (BatchEntry& e : b->entries)
+            for (int q = 0; q < e.n; q++) e.s->pos[q] = e.swap_perm[q];
+        return;
+    }
+    batch_enqueue_work(b, zero_init, st);
+}
+
+double batch_run(hq_batch_s* b, bool zero_init) {
+    cudaStream_t st = ctx().stream;
+    if (!b->ev0) {
+        HQ_CHECK_CUDA(cudaEventCreate(&b->ev0));
+        HQ_CHECK_CUDA(cudaEventCreate(&b->ev1));
+    }
+    HQ_CHECK_CUDA(cudaEventRecord(b->ev0, st));
+    batch_enqueue(b, zero_init);
+    HQ_CHECK_CUDA(cudaEventRecord(b->ev1, st));
+    HQ_CHECK_CUDA(cudaEventSynchronize(b->ev1));
+    check_device_error();
+    float ms = 0.f;
+    HQ_CHECK_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    return double(ms) * 1000.0;
+}
+
+void batch_capture(hq_batch_s* b, bool zero_init) {
+    HQ_REQUIRE(b->compiled, HQ_ERR_STATE, "batch not compiled");
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    // the graph replays on canonical layouts; bring states there first, and
+    // keep the layouts as they are now (capturing runs nothing)
+    if (!zero_init)
+        for (BatchEntry& e : b->entries) state_canonicalize(e.s);
+    std::vector<std::vector<int>> saved;
+    for (const BatchEntry& e : b->entries) saved.push_back(e.s->pos);
+    struct Restore {
+        hq_batch_s* b;
+        std::vector<std::vector<int>>& saved;
+        ~Restore() {
+            for (size_t i = 0; i < b->entries.size(); i++) b->entries[i].s->pos = saved[i];
+        }
+    } restore{b, saved};
+    cudaStream_t cs;
+    HQ_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    try {
+        HQ_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        try {
+            batch_enqueue_work(b, zero_init, cs);
+        } catch (...) {
+            cudaStreamEndCapture(cs, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        HQ_CHECK_CUDA(cudaStreamEndCapture(cs, &g));
+        HQ_CHECK_CUDA(cudaGraphInstantiate(&b->graph, g, 0));
+        cudaGraphDestroy(g);
+    } catch (...) {
+        cudaStreamDestroy(cs);
+        throw;
+    }
+    cudaStreamDestroy(cs);
+    b->graph_zero = zero_init;
+}
+
+}  // namespace hq

@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "batch.h"
 #include "common.h"
 #include "compiler.h"
 #include "device.h"
@@ -417,6 +418,86 @@ hq_status hq_circuit_capture_graph(hq_circuit c, hq_state s) {
     HQ_NONNULL(c);
     HQ_NONNULL(s);
     circuit_capture(c, s);
+    HQ_API_END
+}
+
+// ---- batches ------------------------------------------------------------------------
+
+hq_status hq_batch_create(hq_batch* out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(out);
+    *out = new hq_batch_s();
+    HQ_API_END
+}
+
+hq_status hq_batch_destroy(hq_batch b) {
+    HQ_API_BEGIN
+    if (b) {
+        batch_release(b);
+        if (b->ev0) cudaEventDestroy(b->ev0);
+        if (b->ev1) cudaEventDestroy(b->ev1);
+        delete b;
+    }
+    HQ_API_END
+}
+
+hq_status hq_batch_add(hq_batch b, hq_circuit c, hq_state s, int32_t* index) {
+    HQ_API_BEGIN
+    HQ_NONNULL(b);
+    HQ_NONNULL(c);
+    HQ_NONNULL(s);
+    HQ_REQUIRE(c->n == s->n, HQ_ERR_INVALID, "state has %d qubits, circuit %d", s->n, c->n);
+    for (const BatchEntry& e : b->entries)
+        HQ_REQUIRE(e.s != s, HQ_ERR_INVALID, "state already in the batch");
+    BatchEntry e;
+    e.n = c->n;
+    e.s = s;
+    e.gates = c->gates;
+    b->entries.push_back(std::move(e));
+    batch_release(b);  // needs a new compile
+    if (index) *index = (int32_t)b->entries.size() - 1;
+    HQ_API_END
+}
+
+hq_status hq_batch_compile(hq_batch b, const hq_compile_options* opt) {
+    HQ_API_BEGIN
+    HQ_NONNULL(b);
+    batch_compile(b, opt);
+    HQ_API_END
+}
+
+hq_status hq_batch_run(hq_batch b, int32_t zero_init, double* elapsed_us) {
+    HQ_API_BEGIN
+    HQ_NONNULL(b);
+    const double us = batch_run(b, zero_init != 0);
+    if (elapsed_us) *elapsed_us = us;
+    HQ_API_END
+}
+
+hq_status hq_batch_enqueue(hq_batch b, int32_t zero_init) {
+    HQ_API_BEGIN
+    HQ_NONNULL(b);
+    batch_enqueue(b, zero_init != 0);
+    HQ_API_END
+}
+
+hq_status hq_batch_capture_graph(hq_batch b, int32_t zero_init) {
+    HQ_API_BEGIN
+    HQ_NONNULL(b);
+    batch_capture(b, zero_init != 0);
+    HQ_API_END
+}
+
+hq_status hq_batch_info(hq_batch b, int32_t* num_circuits, int64_t* num_groups,
+                        int64_t* num_items, uint64_t* pass_bytes, int32_t* tile_qubits) {
+    HQ_API_BEGIN
+    HQ_NONNULL(b);
+    if (num_circuits) *num_circuits = (int32_t)b->entries.size();
+    if (num_groups) *num_groups = b->num_groups;
+    if (num_items) *num_items = b->num_items;
+    if (pass_bytes) *pass_bytes = b->pass_bytes;
+    if (tile_qubits)
+        for (size_t i = 0; i < b->entries.size(); i++) tile_qubits[i] = b->entries[i].k;
     HQ_API_END
 }
 

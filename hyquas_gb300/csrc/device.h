@@ -85,7 +85,7 @@ struct OshmProgramHeader {
 };
 
 // Launch parameters passed by value.
-struct OshmLaunch {
+struct alignas(16) OshmLaunch {
     void* state;                // float2*
     const OshmPhase* phases;    // device
     const OshmOp* ops;          // device
@@ -98,6 +98,39 @@ struct OshmLaunch {
     uint32_t piece_slot[32];    // matching smem slot offsets
     uint64_t ntiles;
 };
+
+static_assert(sizeof(OshmLaunch) % 16 == 0, "OshmLaunch is copied as 16-byte words");
+
+// ---- batched OShareMem engine -----------------------------------------------------
+// One persistent launch serves many circuits.  Work items (circuit, group,
+// range of tiles) are handed out in queue order by an atomic counter; an item
+// of group g starts when its circuit's completion counter shows every tile of
+// groups 0..g-1 written.  Items are queued group level by group level, so an
+// item's predecessors were always handed out before it.
+enum : uint32_t {
+    ITEM_FIRST = 1,  // first group of its circuit: may synthesise |0...0> instead of loading
+};
+struct BatchItem {
+    uint32_t group;    // index of the group's OshmLaunch
+    uint32_t circuit;  // completion counter of the circuit
+    uint32_t tile0;    // first tile
+    uint32_t count;    // tiles
+    uint32_t need;     // counter value that must be reached before the item starts
+    uint32_t flags;
+};
+struct BatchLaunch {
+    const OshmLaunch* groups;
+    const BatchItem* items;
+    uint32_t nitems;
+    uint32_t zero_init;  // ITEM_FIRST items start from |0...0> (the state is not read)
+    uint32_t* head;      // next item to hand out
+    uint32_t* done;      // per circuit: tiles finished
+    int* err;
+};
+constexpr int kBatchTile = 13;  // widest tile of the batched kernel (2^13 amplitudes)
+constexpr int kBatchMinTile = 10;  // narrowest: one warp per tile
+void launch_oshm_batch(const BatchLaunch& b, int grid, bool cooperative, void* stream);
+int oshm_batch_slots();  // resident blocks of the batched kernel on this GPU
 
 // ---- launchers (implemented in the .cu files) -------------------------------
 void launch_plain_gate(void* state, int n, const PlainGate& g, void* stream);

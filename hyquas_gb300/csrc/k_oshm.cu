@@ -391,50 +391,16 @@ __device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hd
     }
 }
 
+// Every phase of the group program on one tile staged in `buf` (pieces as
+// loaded; they hold (re0, re1, im0, im1) afterwards).  Thread t of the tile's
+// 2^(p.k-R) threads; threads of the block beyond those pass `active` = false
+// and only take part in the barriers.
 template <int K, int R>
-__global__ void __launch_bounds__(1 << (K - R)) k_oshm(const OshmLaunch p) {
-    constexpr int T = 1 << (K - R);      // threads per tile
-    constexpr int NV = 1 << (R - 1);     // f32x2 vectors per thread (2 amplitudes each)
-    constexpr int PPT = (1 << (K - 1)) / T;  // 16-byte pieces per thread
-    static_assert(PPT >= 1 && PPT <= 32, "piece count");
-    constexpr int TILE4 = 1 << (K - 1);  // float4 pieces per tile buffer
-    extern __shared__ float4 smem4[];     // two tile buffers
-    const int t = threadIdx.x;
-    float2* __restrict__ state = reinterpret_cast<float2*>(p.state);
-
-    // Piece (t + m*T) of a tile holds local amplitudes 2(t + m*T) and +1.
-    const uint64_t toff = local_to_phys(uint32_t(t) << 1, K, p.tile_phys);
-    const uint32_t tslot = swz(uint32_t(t) << 1);
-    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem4);
-
-    // stage tile u into buffer b, as loaded: (re0, im0, re1, im1)
-    auto load_tile = [&](uint64_t u, int b) {
-        const uint64_t tb = tile_base(u, p.nruns, p.run_src, p.run_dst, p.run_len);
-        const float2* __restrict__ gsrc = state + tb + toff;
-        const uint32_t bb = sbase + uint32_t(b) * TILE4 * 16u;
-#pragma unroll
-        for (int m = 0; m < PPT; m++)
-            cp_async16(bb + (tslot ^ p.piece_slot[m]) * 8u, gsrc + p.piece_off[m]);
-        cp_async_commit();
-    };
-
-    // Persistent loop over tiles; the next tile's copy is in flight while the
-    // current one is computed.
-    uint64_t u = blockIdx.x;
-    if (u < p.ntiles) load_tile(u, 0);
-    for (int it = 0; u < p.ntiles; it++, u += gridDim.x) {
-        const uint64_t un = u + gridDim.x;
-        if (un < p.ntiles) {
-            load_tile(un, (it + 1) & 1);
-            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        } else {
-            cp_async_wait_all();
-        }
-        __syncthreads();
-        float4* buf = smem4 + (it & 1) * TILE4;
-        const uint64_t base = tile_base(u, p.nruns, p.run_src, p.run_dst, p.run_len);
-
-        for (int ph = 0; ph < p.nphases; ph++) {
+__device__ __forceinline__ void run_phases(const OshmLaunch& p, float4* buf, uint64_t base, int t,
+                                           bool active) {
+    constexpr int NV = 1 << (R - 1);
+    for (int ph = 0; ph < p.nphases; ph++) {
+        if (active) {
             const OshmPhase P = p.phases[ph];
             uint32_t gl = 0;
             uint64_t gphys = 0;
@@ -507,8 +473,54 @@ __global__ void __launch_bounds__(1 << (K - R)) k_oshm(const OshmLaunch p) {
                     if ((j >> (b - 1)) & 1) s ^= col[b];
                 reinterpret_cast<ulonglong2*>(buf)[s >> 1] = make_ulonglong2(A.re[j], A.im[j]);
             }
-            __syncthreads();
         }
+        __syncthreads();
+    }
+}
+
+template <int K, int R>
+__global__ void __launch_bounds__(1 << (K - R)) k_oshm(const OshmLaunch p) {
+    constexpr int T = 1 << (K - R);      // threads per tile
+    constexpr int PPT = (1 << (K - 1)) / T;  // 16-byte pieces per thread
+    static_assert(PPT >= 1 && PPT <= 32, "piece count");
+    constexpr int TILE4 = 1 << (K - 1);  // float4 pieces per tile buffer
+    extern __shared__ float4 smem4[];     // two tile buffers
+    const int t = threadIdx.x;
+    float2* __restrict__ state = reinterpret_cast<float2*>(p.state);
+
+    // Piece (t + m*T) of a tile holds local amplitudes 2(t + m*T) and +1.
+    const uint64_t toff = local_to_phys(uint32_t(t) << 1, K, p.tile_phys);
+    const uint32_t tslot = swz(uint32_t(t) << 1);
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem4);
+
+    // stage tile u into buffer b, as loaded: (re0, im0, re1, im1)
+    auto load_tile = [&](uint64_t u, int b) {
+        const uint64_t tb = tile_base(u, p.nruns, p.run_src, p.run_dst, p.run_len);
+        const float2* __restrict__ gsrc = state + tb + toff;
+        const uint32_t bb = sbase + uint32_t(b) * TILE4 * 16u;
+#pragma unroll
+        for (int m = 0; m < PPT; m++)
+            cp_async16(bb + (tslot ^ p.piece_slot[m]) * 8u, gsrc + p.piece_off[m]);
+        cp_async_commit();
+    };
+
+    // Persistent loop over tiles; the next tile's copy is in flight while the
+    // current one is computed.
+    uint64_t u = blockIdx.x;
+    if (u < p.ntiles) load_tile(u, 0);
+    for (int it = 0; u < p.ntiles; it++, u += gridDim.x) {
+        const uint64_t un = u + gridDim.x;
+        if (un < p.ntiles) {
+            load_tile(un, (it + 1) & 1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            cp_async_wait_all();
+        }
+        __syncthreads();
+        float4* buf = smem4 + (it & 1) * TILE4;
+        const uint64_t base = tile_base(u, p.nruns, p.run_src, p.run_dst, p.run_len);
+
+        run_phases<K, R>(p, buf, base, t, true);
 
         // write back in place, (re0, re1, im0, im1) -> (re0, im0, re1, im1)
         float2* __restrict__ gdst = state + base + toff;
@@ -527,6 +539,136 @@ __global__ void __launch_bounds__(1 << (K - R)) k_oshm(const OshmLaunch p) {
             *reinterpret_cast<float4*>(gdst + p.piece_off[m]) = out;
         }
         __syncthreads();  // this buffer is refilled two iterations on
+    }
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for *ctr >= need (acquire).  Gives up after about two seconds,
+// or as soon as another block has recorded an error, and returns false; the
+// first block to give up records err = {1, site 8, item}.
+__device__ bool wait_counter(const uint32_t* ctr, uint32_t need, int* err, uint32_t item) {
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t spin = 0;; spin++) {
+        uint32_t v;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+        if (v >= need) return true;
+        if (*reinterpret_cast<volatile int*>(err) != 0) return false;
+        if (spin >= (1u << 24) || globaltimer_ns() - t0 > 2000000000ull) {
+            if (atomicCAS(err, 0, 1) == 0) {
+                err[1] = 8;  // site: batched item dependency wait
+                err[2] = (int)item;
+            }
+            return false;
+        }
+        __nanosleep(128);
+    }
+}
+
+// Batched OShareMem: persistent blocks pull (circuit, group, tile range) items.
+// Tiles of every width k in [10, K] run with R = 5 register qubits: the
+// 2^(k-5) threads of a tile each hold 32 amplitudes and move 16 pieces; the
+// other threads of the block only join the barriers.
+template <int K, int R>
+__global__ void __launch_bounds__(1 << (K - R)) k_oshm_batch(const BatchLaunch b) {
+    constexpr int T = 1 << (K - R);
+    constexpr int PPT = 1 << (R - 1);    // pieces per thread, any tile width
+    constexpr int TILE4 = 1 << (K - 1);
+    extern __shared__ float4 smem4[];
+    __shared__ OshmLaunch sp;            // the current item's group
+    __shared__ uint32_t s_item;
+    __shared__ int s_ok;
+    const int t = threadIdx.x;
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem4);
+    const uint32_t tslot = swz(uint32_t(t) << 1);
+
+    for (;;) {
+        if (t == 0) s_item = atomicAdd(b.head, 1u);
+        __syncthreads();
+        const uint32_t i = s_item;
+        if (i >= b.nitems) return;
+        const BatchItem it = b.items[i];
+        if (t == 0) {
+            bool ok = true;
+            if (it.need) ok = wait_counter(b.done + it.circuit, it.need, b.err, i);
+            __threadfence();
+            s_ok = ok;
+        }
+        {
+            const uint4* src = reinterpret_cast<const uint4*>(b.groups + it.group);
+            for (int w = t; w < int(sizeof(OshmLaunch) / 16); w += T)
+                reinterpret_cast<uint4*>(&sp)[w] = src[w];
+        }
+        __syncthreads();
+        if (!s_ok) return;
+
+        const int kc = sp.k;
+        const bool active = t < (1 << (kc - R));
+        const bool zero = (it.flags & ITEM_FIRST) && b.zero_init;
+        float2* __restrict__ state = reinterpret_cast<float2*>(sp.state);
+        const uint64_t toff = active ? local_to_phys(uint32_t(t) << 1, kc, sp.tile_phys) : 0;
+
+        auto stage = [&](uint64_t u, int bsel) {
+            if (active) {
+                if (zero) {
+                    float4* dst = smem4 + bsel * TILE4;
+#pragma unroll
+                    for (int m = 0; m < PPT; m++)
+                        dst[(tslot ^ sp.piece_slot[m]) >> 1] =
+                            make_float4((u == 0 && t == 0 && m == 0) ? 1.f : 0.f, 0.f, 0.f, 0.f);
+                } else {
+                    const uint64_t tb = tile_base(u, sp.nruns, sp.run_src, sp.run_dst, sp.run_len);
+                    const float2* __restrict__ gsrc = state + tb + toff;
+                    const uint32_t bb = sbase + uint32_t(bsel) * TILE4 * 16u;
+#pragma unroll
+                    for (int m = 0; m < PPT; m++)
+                        cp_async16(bb + (tslot ^ sp.piece_slot[m]) * 8u, gsrc + sp.piece_off[m]);
+                }
+            }
+            cp_async_commit();
+        };
+
+        const uint64_t uend = uint64_t(it.tile0) + it.count;
+        uint64_t u = it.tile0;
+        stage(u, 0);
+        for (int j = 0; u < uend; j++, u++) {
+            if (u + 1 < uend) {
+                stage(u + 1, (j + 1) & 1);
+                asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+            } else {
+                cp_async_wait_all();
+            }
+            __syncthreads();
+            float4* buf = smem4 + (j & 1) * TILE4;
+            const uint64_t base = tile_base(u, sp.nruns, sp.run_src, sp.run_dst, sp.run_len);
+            run_phases<K, R>(sp, buf, base, t, active);
+            if (active) {
+                float2* __restrict__ gdst = state + base + toff;
+                const bool soa = sp.nphases > 0;
+#pragma unroll
+                for (int m = 0; m < PPT; m++) {
+                    const uint32_t piece = (tslot ^ sp.piece_slot[m]) >> 1;
+                    float4 out;
+                    if (soa) {
+                        const ulonglong2 q = reinterpret_cast<const ulonglong2*>(buf)[piece];
+                        vunpack(q.x, out.x, out.z);
+                        vunpack(q.y, out.y, out.w);
+                    } else {
+                        out = buf[piece];
+                    }
+                    *reinterpret_cast<float4*>(gdst + sp.piece_off[m]) = out;
+                }
+            }
+            __syncthreads();
+        }
+        // publish: every thread's stores, then one release of the tile count
+        __threadfence();
+        __syncthreads();
+        if (t == 0) atomicAdd(b.done + it.circuit, it.count);
     }
 }
 
@@ -549,7 +691,42 @@ void launch_k(const OshmLaunch& p, cudaStream_t s) {
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 
+constexpr int kBatchR = 5;
+constexpr size_t kBatchSmem = 2 * (sizeof(float2) << kBatchTile);
+
+int batch_blocks_per_sm() {
+    static int bps = 0;
+    if (!bps) {
+        auto kern = k_oshm_batch<kBatchTile, kBatchR>;
+        HQ_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)kBatchSmem));
+        HQ_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &bps, kern, 1 << (kBatchTile - kBatchR), kBatchSmem));
+        HQ_REQUIRE(bps >= 1, HQ_ERR_UNSUPPORTED, "batched OShareMem kernel does not fit on an SM");
+    }
+    return bps;
+}
+
 }  // namespace
+
+int oshm_batch_slots() { return ctx().sm_count * batch_blocks_per_sm(); }
+
+void launch_oshm_batch(const BatchLaunch& b, int grid, bool cooperative, void* stream) {
+    const int slots = oshm_batch_slots();
+    HQ_REQUIRE(grid >= 1 && grid <= slots, HQ_ERR_INVALID,
+               "batched launch: %d blocks, %d can be resident", grid, slots);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(1u << (kBatchTile - kBatchR));
+    cfg.dynamicSmemBytes = kBatchSmem;
+    cfg.stream = (cudaStream_t)stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = cooperative ? 1 : 0;
+    HQ_CHECK_CUDA(cudaLaunchKernelEx(&cfg, k_oshm_batch<kBatchTile, kBatchR>, b));
+}
 
 uint32_t oshm_swizzle(uint32_t x) { return swz(x); }
 

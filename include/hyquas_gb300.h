@@ -224,6 +224,33 @@ hq_status hq_circuit_enqueue(hq_circuit c, hq_state s);
 hq_status hq_circuit_capture_graph(hq_circuit c, hq_state s);
 hq_status hq_synchronize(void);
 
+/* ---- batched execution (no reference counterpart: the reference runs one
+ * circuit per process, src/circuit.cpp:16-71) ------------------------------
+ * Many circuits of uneven qubit counts run in ONE persistent launch that pulls
+ * (circuit, gate group, tile range) items from a device work queue. */
+typedef struct hq_batch_s* hq_batch;
+hq_status hq_batch_create(hq_batch* out);
+hq_status hq_batch_destroy(hq_batch b);
+/* Add circuit c (its gates are copied; it need not be compiled) to run on
+ * state s (same qubit count; s must outlive the batch's runs). */
+hq_status hq_batch_add(hq_batch b, hq_circuit c, hq_state s, int32_t* index);
+/* Plan every circuit as OShareMem groups and upload one program.  opt may be
+ * NULL; opt->tile_qubits = 0 lets the cost model choose the tile width of
+ * each circuit in [10, 13]; circuits below 10 qubits run gate by gate. */
+hq_status hq_batch_compile(hq_batch b, const hq_compile_options* opt);
+/* One run of every circuit on its state.  zero_init != 0: states start from
+ * |0...0> (written by the first group, never read).  elapsed_us may be NULL. */
+hq_status hq_batch_run(hq_batch b, int32_t zero_init, double* elapsed_us);
+/* Enqueue a run on the library stream without synchronising. */
+hq_status hq_batch_enqueue(hq_batch b, int32_t zero_init);
+/* Capture a run into a CUDA graph; later runs with the same zero_init replay it. */
+hq_status hq_batch_capture_graph(hq_batch b, int32_t zero_init);
+/* num_circuits, total gate groups, work items and pass bytes (2 x 8 B x 2^n
+ * per group summed over circuits); tile_qubits[i] = tile width chosen for
+ * circuit i (0 = gate by gate) when not NULL. */
+hq_status hq_batch_info(hq_batch b, int32_t* num_circuits, int64_t* num_groups,
+                        int64_t* num_items, uint64_t* pass_bytes, int32_t* tile_qubits);
+
 /* ---- single group entry points (the reference kernel ABI, src/kernel.h) -- */
 
 /* One OShareMem pass over the state applying `num_gates` gates (logical
