@@ -57,6 +57,11 @@ class hq_compile_options(C.Structure):
                 ("reference_grouping", C.c_int32), ("specialize", C.c_int32)]
 
 
+class hq_server_options(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("step_budget_us", C.c_double),
+                ("planner_threads", C.c_int32), ("tile_qubits", C.c_int32)]
+
+
 def _load():
     if not LIB_PATH.exists():
         raise ImportError(f"native library missing: {LIB_PATH} (run hyquas_gb300/build.py)")
@@ -80,6 +85,7 @@ def _load():
         "hq_state_prob_zero": [P, I32, C.POINTER(D)],
         "hq_state_norm": [P, C.POINTER(D)],
         "hq_state_marginals": [P, P],
+        "hq_state_sample": [P, I32, U64, P],
         "hq_state_remap": [P, P],
         "hq_apply_gates": [P, P, I32],
         "hq_compile_options_default": [C.POINTER(hq_compile_options)],
@@ -104,6 +110,19 @@ def _load():
         "hq_apply_transmm_group": [P, P, I32, U64, I32],
         "hq_apply_unitary": [P, P, U64, I32],
         "hq_group_unitary": [P, I32, U64, P],
+        "hq_server_options_default": [C.POINTER(hq_server_options)],
+        "hq_server_check": [C.POINTER(hq_server_options), I32, P, I32],
+        "hq_server_create": [C.POINTER(hq_server_options), C.POINTER(P)],
+        "hq_server_destroy": [P],
+        "hq_server_submit": [P, I32, P, I32, C.POINTER(I64)],
+        "hq_server_wait": [P, I64, D, C.POINTER(I32)],
+        "hq_server_poll": [P, P, I32, C.POINTER(I32)],
+        "hq_server_state": [P, I64, C.POINTER(P)],
+        "hq_server_times": [P, I64, C.POINTER(D), C.POINTER(D), C.POINTER(D)],
+        "hq_server_release": [P, I64],
+        "hq_server_steps": [P, I64, C.POINTER(I64), C.POINTER(I64)],
+        "hq_server_stats": [P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64), C.POINTER(U64),
+                            C.POINTER(U64)],
         "hq_batch_create": [C.POINTER(P)],
         "hq_batch_destroy": [P],
         "hq_batch_add": [P, P, P, C.POINTER(I32)],
@@ -289,6 +308,15 @@ class State:
         if zero:
             self.init_zero()
 
+    @classmethod
+    def _borrow(cls, handle, n: int) -> "State":
+        """A view of a state owned by the library (e.g. a served result)."""
+        st = cls.__new__(cls)
+        st.n = n
+        st._h = C.c_void_p(handle)
+        st._borrowed = True
+        return st
+
     @property
     def handle(self):
         return self._h
@@ -334,6 +362,12 @@ class State:
         check(lib.hq_state_marginals(self._h, out.ctypes.data))
         return out
 
+    def sample(self, shots: int, seed: int = 0) -> np.ndarray:
+        """`shots` logical basis indices drawn from |amp|^2 (seeded SplitMix64 draws)."""
+        out = np.empty(max(1, shots), dtype=np.uint64)
+        check(lib.hq_state_sample(self._h, shots, seed, out.ctypes.data))
+        return out[:shots]
+
     def remap(self, new_pos):
         arr = (C.c_int32 * self.n)(*new_pos)
         check(lib.hq_state_remap(self._h, arr))
@@ -356,9 +390,9 @@ class State:
         check(lib.hq_apply_unitary(self._h, u.ctypes.data, group_mask, _PRECISIONS[precision]))
 
     def free(self):
-        if self._h:
+        if self._h and not getattr(self, "_borrowed", False):
             lib.hq_state_destroy(self._h)
-            self._h = C.c_void_p()
+        self._h = C.c_void_p()
 
     def __del__(self):
         try:
@@ -512,6 +546,100 @@ class Circuit:
             pass
 
 
+REQ_STATUS = {0: "planning", 1: "queued", 2: "running", 3: "done", 4: "failed"}
+
+
+def server_options(hbm_budget: int | None = None, step_budget_us: float = 0.0,
+                   planner_threads: int = 0, tile_qubits: int = 0) -> hq_server_options:
+    o = hq_server_options()
+    check(lib.hq_server_options_default(C.byref(o)))
+    if hbm_budget is not None:
+        o.hbm_budget = hbm_budget
+    if step_budget_us:
+        o.step_budget_us = step_budget_us
+    if planner_threads:
+        o.planner_threads = planner_threads
+    o.tile_qubits = tile_qubits
+    return o
+
+
+def server_check(n: int, gates, **kw):
+    """Host-only admission checks of a request (raises HQError)."""
+    o = server_options(**kw)
+    arr = gate_array(gates)
+    check(lib.hq_server_check(C.byref(o), n, arr, len(gates)))
+
+
+class Server:
+    """Request loop: submit circuits, get results back as they finish.
+
+    Arriving requests are admitted while their states fit `hbm_budget` and
+    run in continuous batches (one persistent launch per step over every
+    admitted request's next gate groups)."""
+
+    def __init__(self, hbm_budget: int | None = None, step_budget_us: float = 0.0,
+                 planner_threads: int = 0, tile_qubits: int = 0):
+        self._h = C.c_void_p()
+        o = server_options(hbm_budget, step_budget_us, planner_threads, tile_qubits)
+        check(lib.hq_server_create(C.byref(o), C.byref(self._h)))
+        self._n: dict[int, int] = {}
+
+    def submit(self, n: int, gates) -> int:
+        """gates: Gate objects, or an array made by gate_array() beforehand."""
+        arr = gates if isinstance(gates, C.Array) else gate_array(gates)
+        rid = C.c_int64()
+        check(lib.hq_server_submit(self._h, n, arr, len(gates), C.byref(rid)))
+        self._n[rid.value] = n
+        return rid.value
+
+    def wait(self, rid: int, timeout: float = 60.0) -> str:
+        st = C.c_int32()
+        check(lib.hq_server_wait(self._h, rid, timeout, C.byref(st)))
+        return REQ_STATUS[st.value]
+
+    def poll(self, cap: int = 4096) -> list[int]:
+        ids = (C.c_int64 * cap)()
+        k = C.c_int32()
+        check(lib.hq_server_poll(self._h, ids, cap, C.byref(k)))
+        return list(ids[: k.value])
+
+    def state(self, rid: int) -> State:
+        h = C.c_void_p()
+        check(lib.hq_server_state(self._h, rid, C.byref(h)))
+        return State._borrow(h.value, self._n[rid])
+
+    def times(self, rid: int) -> tuple[float, float, float]:
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        check(lib.hq_server_times(self._h, rid, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def steps(self, rid: int) -> tuple[int, int]:
+        """(first, last) step index the request's work ran in."""
+        a, b = C.c_int64(), C.c_int64()
+        check(lib.hq_server_steps(self._h, rid, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def release(self, rid: int):
+        check(lib.hq_server_release(self._h, rid))
+
+    def stats(self) -> dict:
+        v = [C.c_int64(), C.c_int64(), C.c_int64(), C.c_uint64(), C.c_uint64()]
+        check(lib.hq_server_stats(self._h, *[C.byref(x) for x in v]))
+        return dict(zip(["steps", "items", "finished", "resident_bytes", "peak_resident_bytes"],
+                        [x.value for x in v]))
+
+    def close(self):
+        if self._h:
+            lib.hq_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Batch:
     """Many circuits (uneven qubit counts) in one persistent launch.
 
@@ -573,5 +701,5 @@ class Batch:
             pass
 
 
-__all__ = ["Circuit", "Batch", "Gate", "State", "ResultItem", "HQError", "init", "device_info",
+__all__ = ["Circuit", "Batch", "Server", "Gate", "State", "ResultItem", "HQError", "init", "device_info",
            "group_unitary", "set_hbm_budget", "hbm_in_use", "lib", "LIB_PATH"]

@@ -35,12 +35,14 @@ double batch_cost(const Partition& part, const std::vector<hq_gate>& gates, int 
     return t + items * kItemSec / std::max(1, slots);
 }
 
-uint32_t chunk_tiles(uint64_t tiles, int slots) {
-    uint64_t c = tiles / (4 * uint64_t(std::max(1, slots)));
-    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 1), 16);
-}
-
 }  // namespace
+
+// Tiles per work item: about four items per resident block and level, at most
+// 64 tiles (4 MiB of amplitudes) per item.
+uint32_t batch_chunk_tiles(uint64_t tiles, int slots) {
+    const uint64_t c = tiles / (4 * uint64_t(std::max(1, slots)));
+    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 1), 64);
+}
 
 void batch_release(hq_batch_s* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -139,7 +141,7 @@ void batch_compile(hq_batch_s* b, const hq_compile_options* opt) {
             const uint64_t tiles = uint64_t(1) << (e.n - e.k);
             HQ_REQUIRE(tiles * e.ngroups < (uint64_t(1) << 32), HQ_ERR_UNSUPPORTED,
                        "batch: circuit %u has too many tiles for the 32-bit item counters", ci);
-            const uint32_t ch = chunk_tiles(tiles, slots);
+            const uint32_t ch = batch_chunk_tiles(tiles, slots);
             for (uint64_t u = 0; u < tiles; u += ch) {
                 BatchItem it;
                 it.group = e.group0 + g;

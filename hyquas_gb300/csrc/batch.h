@@ -42,6 +42,7 @@ struct hq_batch_s {
 
 namespace hq {
 
+uint32_t batch_chunk_tiles(uint64_t tiles, int slots);
 void batch_compile(hq_batch_s* b, const hq_compile_options* opt);
 void batch_release(hq_batch_s* b);
 void batch_enqueue(hq_batch_s* b, bool zero_init);

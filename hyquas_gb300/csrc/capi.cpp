@@ -14,6 +14,7 @@
 #include "device.h"
 #include "executor.h"
 #include "gates.h"
+#include "server.h"
 
 namespace hq {
 const std::string& last_error();
@@ -186,6 +187,15 @@ hq_status hq_state_marginals(hq_state s, double* p1) {
     double h[1 + 64];
     state_marginals(s, h);
     for (int q = 0; q < s->n; q++) p1[q] = h[1 + s->pos[q]];
+    HQ_API_END
+}
+
+hq_status hq_state_sample(hq_state s, int32_t shots, uint64_t seed, uint64_t* out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_REQUIRE(shots >= 0, HQ_ERR_INVALID, "negative shot count");
+    if (shots > 0) HQ_NONNULL(out);
+    state_sample(s, shots, seed, out);
     HQ_API_END
 }
 
@@ -498,6 +508,131 @@ hq_status hq_batch_info(hq_batch b, int32_t* num_circuits, int64_t* num_groups,
     if (pass_bytes) *pass_bytes = b->pass_bytes;
     if (tile_qubits)
         for (size_t i = 0; i < b->entries.size(); i++) tile_qubits[i] = b->entries[i].k;
+    HQ_API_END
+}
+
+// ---- serving ------------------------------------------------------------------------
+
+hq_status hq_server_options_default(hq_server_options* opt) {
+    HQ_API_BEGIN
+    HQ_NONNULL(opt);
+    std::memset(opt, 0, sizeof(*opt));
+    opt->hbm_budget = 150ull * 1000 * 1000 * 1000;
+    opt->step_budget_us = 2000.0;
+    opt->planner_threads = 4;
+    opt->tile_qubits = 0;
+    HQ_API_END
+}
+
+hq_status hq_server_check(const hq_server_options* opt, int32_t num_qubits, const hq_gate* gates,
+                          int32_t num_gates) {
+    HQ_API_BEGIN
+    HQ_NONNULL(opt);
+    server_check(*opt, num_qubits, gates, num_gates);
+    HQ_API_END
+}
+
+hq_status hq_server_create(const hq_server_options* opt, hq_server* out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(out);
+    hq_server_options o;
+    if (opt) {
+        o = *opt;
+    } else {
+        hq_server_options_default(&o);
+    }
+    HQ_REQUIRE(o.tile_qubits == 0 || (o.tile_qubits >= kBatchMinTile && o.tile_qubits <= kBatchTile),
+               HQ_ERR_INVALID, "tile_qubits %d outside [%d, %d]", o.tile_qubits, kBatchMinTile,
+               kBatchTile);
+    *out = server_create(o);
+    HQ_API_END
+}
+
+hq_status hq_server_destroy(hq_server sv) {
+    HQ_API_BEGIN
+    if (sv) server_destroy(sv);
+    HQ_API_END
+}
+
+hq_status hq_server_submit(hq_server sv, int32_t num_qubits, const hq_gate* gates,
+                           int32_t num_gates, int64_t* id) {
+    HQ_API_BEGIN
+    HQ_NONNULL(sv);
+    const int64_t v = server_submit(sv, num_qubits, gates, num_gates);
+    if (id) *id = v;
+    HQ_API_END
+}
+
+hq_status hq_server_wait(hq_server sv, int64_t id, double timeout_s, int32_t* status) {
+    HQ_API_BEGIN
+    HQ_NONNULL(sv);
+    const int st = server_wait(sv, id, timeout_s);
+    if (status) *status = st;
+    HQ_API_END
+}
+
+hq_status hq_server_poll(hq_server sv, int64_t* ids, int32_t cap, int32_t* count) {
+    HQ_API_BEGIN
+    HQ_NONNULL(sv);
+    HQ_REQUIRE(cap >= 0 && (cap == 0 || ids), HQ_ERR_INVALID, "bad id buffer");
+    const int k = server_poll(sv, ids, cap);
+    if (count) *count = k;
+    HQ_API_END
+}
+
+hq_status hq_server_state(hq_server sv, int64_t id, hq_state* out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(sv);
+    HQ_NONNULL(out);
+    std::lock_guard<std::mutex> lk(sv->mu);
+    Request* r = server_find(sv, id);
+    HQ_REQUIRE(r->status != HQ_REQ_FAILED, HQ_ERR_STATE, "request %lld failed: %s", (long long)id,
+               r->error.c_str());
+    HQ_REQUIRE(r->status == HQ_REQ_DONE, HQ_ERR_BUSY, "request %lld not finished", (long long)id);
+    HQ_REQUIRE(!r->released && r->state, HQ_ERR_STATE, "request %lld released", (long long)id);
+    *out = r->state;
+    HQ_API_END
+}
+
+hq_status hq_server_times(hq_server sv, int64_t id, double* submit_us, double* admit_us,
+                          double* done_us) {
+    HQ_API_BEGIN
+    HQ_NONNULL(sv);
+    std::lock_guard<std::mutex> lk(sv->mu);
+    Request* r = server_find(sv, id);
+    if (submit_us) *submit_us = r->t_submit;
+    if (admit_us) *admit_us = r->t_admit;
+    if (done_us) *done_us = r->t_done;
+    HQ_API_END
+}
+
+hq_status hq_server_steps(hq_server sv, int64_t id, int64_t* first_step, int64_t* last_step) {
+    HQ_API_BEGIN
+    HQ_NONNULL(sv);
+    std::lock_guard<std::mutex> lk(sv->mu);
+    Request* r = server_find(sv, id);
+    if (first_step) *first_step = r->first_step;
+    if (last_step) *last_step = r->last_step;
+    HQ_API_END
+}
+
+hq_status hq_server_release(hq_server sv, int64_t id) {
+    HQ_API_BEGIN
+    HQ_NONNULL(sv);
+    server_release(sv, id);
+    HQ_API_END
+}
+
+hq_status hq_server_stats(hq_server sv, int64_t* steps, int64_t* items, int64_t* finished,
+                          uint64_t* resident_bytes, uint64_t* peak_resident_bytes) {
+    HQ_API_BEGIN
+    HQ_NONNULL(sv);
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (steps) *steps = sv->steps;
+    if (items) *items = sv->items;
+    if (finished) *finished = sv->ndone;
+    if (resident_bytes) *resident_bytes = sv->resident;
+    if (peak_resident_bytes) *peak_resident_bytes = sv->peak_resident;
     HQ_API_END
 }
 

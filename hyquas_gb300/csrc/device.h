@@ -132,6 +132,14 @@ constexpr int kBatchMinTile = 10;  // narrowest: one warp per tile
 void launch_oshm_batch(const BatchLaunch& b, int grid, bool cooperative, void* stream);
 int oshm_batch_slots();  // resident blocks of the batched kernel on this GPU
 
+// ---- sampling (k_sample.cu) ----------------------------------------------------------
+constexpr int kSampleBlockBits = 12;  // amplitudes per block of the cumulative distribution
+size_t sample_scratch_doubles(int n);
+uint64_t sample_mix64(uint64_t z);   // SplitMix64 output function
+// Block CDF into d_cdf, then `shots` physical indices into d_out.
+void launch_sample(const void* state, int n, int shots, uint64_t seed, double* d_cdf,
+                   uint64_t* d_out, void* stream);
+
 // ---- launchers (implemented in the .cu files) -------------------------------
 void launch_plain_gate(void* state, int n, const PlainGate& g, void* stream);
 void launch_init_zero(void* state, int n, void* stream);

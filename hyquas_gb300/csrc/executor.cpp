@@ -10,7 +10,7 @@ namespace hq {
 
 // ---- states ---------------------------------------------------------------------
 
-static size_t marg_scratch_doubles(int n) {
+size_t state_scratch_doubles(int n) {
     const uint64_t nquads = (uint64_t(1) << n) / 2;
     const uint64_t nb1 = (nquads + 2047) / 2048;
     const uint64_t nb2 = (nb1 + 4095) / 4096;
@@ -27,7 +27,7 @@ hq_state_s* state_create(int n) {
     for (int q = 0; q < n; q++) s->pos[q] = q;
     try {
         s->d = dev_alloc(s->bytes);
-        s->scratch_doubles = marg_scratch_doubles(n);
+        s->scratch_doubles = state_scratch_doubles(n);
         s->d_scratch = (double*)dev_alloc(sizeof(double) * s->scratch_doubles);
     } catch (...) {
         if (s->d) dev_free(s->d, s->bytes);
@@ -128,6 +128,40 @@ static PlainGate lower_plain(const hq_gate& g, const std::vector<int>& pos) {
     else
         p.kind = PK_GENERAL;
     return p;
+}
+
+void state_sample(hq_state_s* s, int shots, uint64_t seed, uint64_t* out) {
+    HQ_REQUIRE(shots >= 0, HQ_ERR_INVALID, "negative shot count");
+    // the inverse CDF runs in logical index order, so draws do not depend on the layout
+    state_canonicalize(s);
+    const int n = s->n;
+    const size_t nb = sample_scratch_doubles(n);
+    const size_t bytes = sizeof(double) * nb + sizeof(uint64_t) * size_t(std::max(shots, 1));
+    char* buf = (char*)dev_alloc(bytes);
+    cudaStream_t st = ctx().stream;
+    std::vector<uint64_t> phys(size_t(std::max(shots, 1)));
+    double total = 0.0;
+    try {
+        double* cdf = (double*)buf;
+        uint64_t* d_out = (uint64_t*)(buf + sizeof(double) * nb);
+        launch_sample(s->d, n, shots, seed, cdf, d_out, st);
+        HQ_CHECK_CUDA(cudaMemcpyAsync(&total, cdf + nb - 1, sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (shots > 0)
+            HQ_CHECK_CUDA(cudaMemcpyAsync(phys.data(), d_out, sizeof(uint64_t) * shots,
+                                          cudaMemcpyDeviceToHost, st));
+        HQ_CHECK_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+        dev_free(buf, bytes);
+        throw;
+    }
+    dev_free(buf, bytes);
+    HQ_REQUIRE(total > 0.0, HQ_ERR_STATE, "sample: the state has zero norm");
+    for (int i = 0; i < shots; i++) {
+        uint64_t l = 0;
+        for (int q = 0; q < n; q++)
+            if ((phys[i] >> s->pos[q]) & 1) l |= uint64_t(1) << q;
+        out[i] = l;
+    }
 }
 
 void apply_plain(hq_state_s* s, const std::vector<hq_gate>& gates) {

@@ -75,6 +75,9 @@ void state_canonicalize(hq_state_s* s);
 void state_remap(hq_state_s* s, const std::vector<int>& new_pos);
 void state_gather(hq_state_s* s, const uint64_t* logical_idx, int64_t count, float* out);
 void state_marginals(hq_state_s* s, double* h_out);  // [total, p1(phys bit b)]
+// `shots` outcomes (logical basis indices) drawn from |amp|^2 with a seeded stream.
+void state_sample(hq_state_s* s, int shots, uint64_t seed, uint64_t* out);
+size_t state_scratch_doubles(int n);  // FP64 reduction scratch a state carries
 
 void apply_plain(hq_state_s* s, const std::vector<hq_gate>& gates);
 void apply_oshm_group(hq_state_s* s, const std::vector<hq_gate>& gates, uint64_t tile_mask_logical);

@@ -126,6 +126,12 @@ hq_status hq_state_prob_zero(hq_state s, int32_t logical_qubit, double* p0);
 hq_status hq_state_norm(hq_state s, double* norm);
 /* P(qubit q = 1) for every logical qubit, one FP64 pass. */
 hq_status hq_state_marginals(hq_state s, double* p1);
+/* Draw `shots` outcomes from |amp|^2: out[i] = logical basis index.  The
+ * draws are the SplitMix64 stream of `seed` (u = output >> 11 scaled to
+ * [0, 1)), inverted through an FP64 cumulative distribution in logical
+ * index order (the state is brought to the identity layout first).  No reference
+ * counterpart (it measures one qubit, src/kernelSimple.cu:497-516). */
+hq_status hq_state_sample(hq_state s, int32_t shots, uint64_t seed, uint64_t* out);
 /* Allocation-free form of hq_state_marginals, for callers that cannot call
  * cudaMalloc: code whose device memory belongs to another allocator (a
  * framework's caching pool, or an HBM budget already handed out in full) and
@@ -250,6 +256,59 @@ hq_status hq_batch_capture_graph(hq_batch b, int32_t zero_init);
  * circuit i (0 = gate by gate) when not NULL. */
 hq_status hq_batch_info(hq_batch b, int32_t* num_circuits, int64_t* num_groups,
                         int64_t* num_items, uint64_t* pass_bytes, int32_t* tile_qubits);
+
+/* ---- serving (no reference counterpart: one circuit per process there,
+ * src/main.cpp:12-230) -------------------------------------------------------
+ * A request loop: submit() returns at once; planner threads partition and
+ * lower each circuit; an engine thread admits planned requests in arrival
+ * order while their state bytes (2^n x 8 B) fit hbm_budget and runs steps,
+ * each step one persistent batched launch over the next gate groups of every
+ * admitted request (continuous batching).  Results stay resident until
+ * hq_server_release. */
+typedef struct hq_server_s* hq_server;
+#define HQ_REQ_PLANNING 0
+#define HQ_REQ_QUEUED 1   /* planned, waiting for memory */
+#define HQ_REQ_RUNNING 2
+#define HQ_REQ_DONE 3
+#define HQ_REQ_FAILED 4
+typedef struct hq_server_options {
+    uint64_t hbm_budget;     /* bytes of resident states admitted at once; 0 = no limit */
+    double step_budget_us;   /* estimated device time of one step, split evenly between
+                                the admitted requests; a request whose next group is
+                                over its share runs a slice of that group's tiles (0 = 2000) */
+    int32_t planner_threads; /* 0 = 4 */
+    int32_t tile_qubits;     /* 0 = 13 (or n when smaller); else 10..13 */
+} hq_server_options;
+/* Defaults: 150 GB budget, 2000 us steps, 4 planners, tile 13. */
+hq_status hq_server_options_default(hq_server_options* opt);
+/* Host-only admission checks of a request (qubit range 10..34, gate indices,
+ * state bytes against the budget); the checks hq_server_submit makes. */
+hq_status hq_server_check(const hq_server_options* opt, int32_t num_qubits, const hq_gate* gates,
+                          int32_t num_gates);
+hq_status hq_server_create(const hq_server_options* opt, hq_server* out);
+/* Stops the engine (the step in flight completes) and frees every state. */
+hq_status hq_server_destroy(hq_server sv);
+hq_status hq_server_submit(hq_server sv, int32_t num_qubits, const hq_gate* gates,
+                           int32_t num_gates, int64_t* id);
+/* Wait up to timeout_s for request id to finish; *status = HQ_REQ_*. */
+hq_status hq_server_wait(hq_server sv, int64_t id, double timeout_s, int32_t* status);
+/* Ids finished (done or failed) since the last call, at most cap of them. */
+hq_status hq_server_poll(hq_server sv, int64_t* ids, int32_t cap, int32_t* count);
+/* The finished request's state (borrowed: valid until hq_server_release; do
+ * not destroy it).  HQ_ERR_BUSY while queued or running; a failed request
+ * returns its error. */
+hq_status hq_server_state(hq_server sv, int64_t id, hq_state* out);
+/* Host clock (microseconds since the server started) of submit, admission
+ * and completion. */
+hq_status hq_server_times(hq_server sv, int64_t id, double* submit_us, double* admit_us,
+                          double* done_us);
+/* Index of the first and last step (batched launch) the request ran in; two
+ * requests whose ranges meet shared a launch. */
+hq_status hq_server_steps(hq_server sv, int64_t id, int64_t* first_step, int64_t* last_step);
+/* Frees the request's state (finished requests only). */
+hq_status hq_server_release(hq_server sv, int64_t id);
+hq_status hq_server_stats(hq_server sv, int64_t* steps, int64_t* items, int64_t* finished,
+                          uint64_t* resident_bytes, uint64_t* peak_resident_bytes);
 
 /* ---- single group entry points (the reference kernel ABI, src/kernel.h) -- */
 

@@ -133,3 +133,31 @@ def compare(ref: np.ndarray, got: np.ndarray) -> dict:
     ov = np.vdot(r, g)
     fid = abs(ov) ** 2 / (np.vdot(r, r).real * np.vdot(g, g).real)
     return {"max_abs_err": err, "one_minus_fidelity": float(1.0 - fid)}
+
+
+def _mix64_uniforms(seed: int, shots: int) -> np.ndarray:
+    """The SplitMix64 stream of `seed` (Steele, Lea, Flood 2014), 53-bit
+    uniforms in [0, 1): the draws the product sampler makes."""
+    mask = (1 << 64) - 1
+    s = seed & mask
+    out = np.empty(shots, dtype=np.float64)
+    for i in range(shots):
+        s = (s + 0x9E3779B97F4A7C15) & mask
+        z = s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & mask
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & mask
+        z ^= z >> 31
+        out[i] = (z >> 11) * (1.0 / (1 << 53))
+    return out
+
+
+def sample(amps: np.ndarray, shots: int, seed: int) -> np.ndarray:
+    """Inverse-CDF sampling of basis indices from |amp|^2 in FP64 with the
+    same draws as hq_state_sample (first index whose cumulative probability
+    exceeds u * total)."""
+    a = np.asarray(amps)
+    p = a.real.astype(np.float64) ** 2 + a.imag.astype(np.float64) ** 2
+    cdf = np.cumsum(p)
+    u = _mix64_uniforms(seed, shots)
+    idx = np.searchsorted(cdf, u * cdf[-1], side="right")
+    return np.minimum(idx, a.size - 1).astype(np.uint64)
