@@ -1,13 +1,15 @@
 #!/usr/bin/env python3
-"""Benchmark: 30-qubit random grid circuit (5x6, 20 cycles) on one GB300.
+"""Benchmarks on one GB300 (default: the 30-qubit random grid circuit).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload grid30|plain20|qft28|batch|serve]
                     [--backend oshm|hybrid|transmm] [--no-cpu-baseline]
 
-A step = one full circuit (845 gates: sqrt(X)/sqrt(Y)/T per qubit and CZ on
-the cycle's coupler pattern) applied to a complex64 state resident in HBM
-(2^30 amplitudes = 8 GiB, larger than L2, so no flush is needed).  `value` is
-circuits per second over all ranks; ms_per_step is device time per circuit.
+grid30 (default, the headline): a step = one full circuit (845 gates:
+sqrt(X)/sqrt(Y)/T per qubit and CZ on the cycle's coupler pattern) applied to a
+complex64 state resident in HBM (2^30 amplitudes = 8 GiB, larger than L2, so no
+flush is needed).  `value` is circuits per second over all ranks;
+ms_per_step is device time per circuit.
 
   roofline      the OShareMem kernel: algorithmic bytes per launch (read + write
                 of every amplitude = 16 * 2^30 B) over its mean launch time,
@@ -23,6 +25,18 @@ circuits per second over all ranks; ms_per_step is device time per circuit.
   --impl reference   the same CPU port as the reference arm (the reference
                 has no CPU implementation of the path; its GPU build needs
                 sources that are not on the GPU machine).
+
+The other workloads print one line each with their own metric:
+  plain20  20 qubits, 10 layers of U3 on every qubit + CNOT matching, plain
+           gate-by-gate path (the state is 8 MiB and L2-resident).
+  qft28    28-qubit QFT on a seeded random state: TransMM groups k = 6, 7, 8 in
+           split-BF16 (3 products), TF32 and FP32 SIMT, with max |d amp| and
+           1 - fidelity against the exact transform.
+  batch    512 circuits (n 10..22, depth 8..40, RY/RZ + CZ) in one persistent
+           launch, against each circuit run alone.
+  serve    Poisson streams at 200, 1000 and 5000 circuits/s (n log-uniform
+           12..32, depth 10..60) through the request loop; circuits/s and
+           p50/p99 latency against one-at-a-time execution.
 
 Multi-GPU: replicas only (the single-GPU path does not shard); each rank runs
 its own circuit on its own GPU, barrier + max over ranks.
@@ -136,12 +150,20 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+_CPU_STATE: dict = {}
+
+
 def cpu_sample(n: int, desc, budget_s: float, threads: int):
     """Time the oracle's complex64 gate-by-gate port on the first gates of the
-    circuit; returns (seconds per gate, gates run)."""
+    circuit; returns (seconds per gate, gates run).  The state buffer is made
+    once per qubit count."""
     import oracle as O
-    state = np.zeros(1 << n, dtype=np.complex64)
-    state[0] = 1
+    state = _CPU_STATE.get(n)
+    if state is None:
+        state = np.zeros(1 << n, dtype=np.complex64)
+        state[0] = 1
+        _CPU_STATE.clear()
+        _CPU_STATE[n] = state
     k = 0
     t_total = 0.0
     # warm one gate (first touch of the 8 GiB buffer is not the algorithm)
@@ -238,7 +260,7 @@ def run_ours(args, dist: Dist):
         traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "kernel": "k_oshm<13,5>" if oshm_t else "transmm",
+                "kernel": "hq_oshm_group (generated per group)" if oshm_t else "k_transmm_tc",
                 "peak_source": peak_kind,
                 "launches_per_circuit": len(dom)}
 
@@ -298,6 +320,350 @@ def run_ours(args, dist: Dist):
         print(json.dumps(line), flush=True)
 
 
+def base_line(args, dist, metric, value, unit, ms, hib, workload, extra_cfg=None):
+    cfg = {"workload": workload, "parallelism": f"replicas x{dist.ws}"}
+    cfg.update(extra_cfg or {})
+    return {"metric": metric, "value": value, "unit": unit, "n_gpus": dist.ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": hib, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic", "config": cfg}
+
+
+def run_plain20(args, dist: Dist):
+    """Config 1: 20 qubits, plain gate-by-gate path, |0..0>, full state out."""
+    import hyquas_gb300 as hq
+    from hyquas_gb300 import workloads as W
+    import oracle as O
+    hq.init(dist.local)
+    n = 20
+    desc = W.plain_u3_cnot(1, n, 10)
+    gates = W.to_gates(desc)
+    circ = hq.Circuit(n)
+    circ.addGates(gates)
+    circ.compile("plain")
+    state = hq.State(n)
+    flush = hq.State(28)  # 2 GiB written between steps: the state is L2-sized
+    for _ in range(args.warmup):
+        state.init_zero()
+        circ.run_on(state)
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    clocks.start()
+    dev = []
+    for _ in range(args.steps):
+        flush.init_zero()
+        state.init_zero()
+        dev.append(circ.run_on(state))
+    clk = clocks.stop()
+    dist.barrier()
+    total_s = dist.max(sum(dev) * 1e-6)
+    value = dist.ws * args.steps / total_s
+    ref = O.run_f64(n, desc)
+    got = state.store()
+    err = O.compare(ref, got)
+    peak, peak_kind = measured_peaks()
+    per_gate_s = total_s / args.steps / len(desc)
+    achieved = 16.0 * (1 << n) / per_gate_s / 1e9
+    pinned = hq.PinnedBuffer(1 << n)
+    e2e = []
+    h2d = 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        c2 = hq.Circuit(n)
+        c2.addGates(gates)
+        c2.compile("plain")
+        state.init_zero()
+        c2.run_on(state)
+        state.store(pinned.array)
+        e2e.append(time.perf_counter() - t0)
+        h2d = sum(64 for _ in gates)  # gate records passed by value per launch
+    pinned.free()
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        a = O.zero_state(n, np.complex64)
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < min(args.cpu_budget, 10.0) or reps == 0:
+            O.apply_f32(n, a, desc, threads=threads)
+            reps += 1
+        cpu = {"value": reps / (time.perf_counter() - t0), "unit": "circuits/s", "cores": threads,
+               "kind": "port", "sample": f"{reps} full circuits (complex64 OpenMP gate by gate)"}
+    line = base_line(args, dist, "20q plain U3+CNOT circuit throughput (circuits/s)", value,
+                     "circuits/s", total_s * 1000 / args.steps, True,
+                     "plain path, 20 qubits, 10 layers of U3 on every qubit + CNOT on a random "
+                     "matching (200 1q + 100 2q gates), |0..0>",
+                     {"l2": "state 8 MiB is L2-resident; a 2 GiB buffer is written between steps",
+                      "max_abs_err": err["max_abs_err"],
+                      "one_minus_fidelity": err["one_minus_fidelity"]})
+    line.update({
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "kernel": "k_plain_gate",
+                     "peak_source": peak_kind,
+                     "note": "per-gate passes over an L2-resident 8 MiB state: frac above 1 "
+                             "measures L2, not HBM"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": dist.ws * args.steps / dist.max(sum(e2e)), "unit": "circuits/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(8 << n)},
+        "gpu_launches": (len(desc) + 1) * args.steps, "clocks": clk})
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_qft28(args, dist: Dist):
+    """Config 3: QFT-28 precision sweep on a seeded random state."""
+    import hyquas_gb300 as hq
+    from hyquas_gb300 import workloads as W
+    hq.init(dist.local)
+    n = args.qft_qubits
+    desc = W.qft(n)
+    gates = W.to_gates(desc)
+    psi = W.random_state(3, n)
+    N = 1 << n
+    # exact transform: QFT|x> = sum_k e^{2 pi i x k / N} |k> / sqrt(N)
+    ref = np.fft.ifft(psi.astype(np.complex128)) * np.sqrt(N)
+    refn = np.vdot(ref, ref).real
+    state = hq.State(n, zero=False)
+    out = np.empty(N, dtype=np.complex64)
+    sweep = []
+    cases = [("oshm", 0, "fp32")]
+    for k in (6, 7, 8):
+        for prec in ("bf16x3", "tf32", "fp32"):
+            cases.append(("transmm", k, prec))
+    best = None
+    for backend, k, prec in cases:
+        rec = {"backend": backend, "k": k, "precision": prec}
+        try:
+            c = hq.Circuit(n)
+            c.addGates(gates)
+            if backend == "oshm":
+                c.compile("oshm")
+            else:
+                c.compile("transmm", mm_qubits=k, precision=prec)
+            ts = []
+            for i in range(max(args.warmup, 1) + args.steps):
+                state.load(psi)
+                t = c.run_on(state)
+                if i >= max(args.warmup, 1):
+                    ts.append(t)
+            state.store(out)
+            g = out.astype(np.complex128)
+            ov = np.vdot(ref, g)
+            rec.update({"ms": float(np.mean(ts)) / 1000.0, "passes": len(c.schedule()),
+                        "max_abs_err": float(np.max(np.abs(g - ref))),
+                        "one_minus_fidelity": float(1 - abs(ov) ** 2 / (refn * np.vdot(g, g).real))})
+            if backend == "transmm" and prec == "bf16x3" and k == 6:
+                best = rec
+        except hq.HQError as e:
+            rec["not_built"] = str(e)
+        sweep.append(rec)
+        if dist.rank == 0:
+            print(json.dumps({"qft_case": rec}), file=sys.stderr, flush=True)
+    value = best["ms"] if best else None
+    peak, peak_kind = measured_peaks()
+    achieved = (best["passes"] * 16.0 * N / (best["ms"] * 1e-3) / 1e9) if best else None
+    line = base_line(args, dist, f"{n}q QFT time (ms), TransMM split-BF16 k=6", value, "ms", value,
+                     False, f"QFT-{n} (H + CU1 for all pairs + swaps folded into the layout) on an "
+                     "iid complex Gaussian normalised state; reference = exact transform (FP64 FFT)",
+                     {"sweep": sweep})
+    line.update({"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                              "frac": achieved / peak if achieved else None, "traffic": None,
+                              "kernel": "k_transmm_tc (circuit average)", "peak_source": peak_kind},
+                 "cpu_baseline": None, "e2e": None,
+                 "gpu_launches": best["passes"] * args.steps if best else None})
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_batch(args, dist: Dist):
+    """Config 4: 512 circuits in one persistent launch vs each alone."""
+    import hyquas_gb300 as hq
+    from hyquas_gb300 import workloads as W
+    import oracle as O
+    hq.init(dist.local)
+    circuits = W.batched(4 + dist.rank, args.batch_count)
+    arrays = [W.to_gates(d) for _, d in circuits]
+    t0 = time.perf_counter()
+    b = hq.Batch()
+    states, circs = [], []
+    for (n, _), g in zip(circuits, arrays):
+        c = hq.Circuit(n)
+        c.addGates(g)
+        s = hq.State(n, zero=False)
+        b.add(c, s)
+        states.append(s)
+        circs.append(c)
+    b.compile()
+    compile_s = time.perf_counter() - t0
+    info = b.info()
+    b.capture_graph(True)
+    for _ in range(args.warmup):
+        b.run()
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    clocks.start()
+    dev = [b.run() for _ in range(args.steps)]
+    clk = clocks.stop()
+    dist.barrier()
+    total_s = dist.max(sum(dev) * 1e-6)
+    value = dist.ws * len(circuits) * args.steps / total_s
+    # correctness: the smallest circuits against the FP64 oracle, all norms
+    order = sorted(range(len(circuits)), key=lambda i: circuits[i][0])
+    errs = [O.compare(O.run_f64(*circuits[i]), states[i].store())["max_abs_err"] for i in order[:8]]
+    norm_dev = max(abs(s.norm() - 1.0) for s in states)
+    # each circuit alone (same kernels: compiled schedule, one launch per group)
+    for c in circs:
+        c.compile("oshm", specialize=0)
+    for c, s in zip(circs[:4], states[:4]):
+        c.run_on(s)
+    hq.synchronize()
+    w0 = time.perf_counter()
+    alone_dev = sum(c.run_on(s) for c, s in zip(circs, states))
+    alone_wall = time.perf_counter() - w0
+    peak, peak_kind = measured_peaks()
+    achieved = info["pass_bytes"] / (total_s / args.steps) / 1e9
+    # e2e: build, plan, run and read every state back to pinned host memory
+    e2e = []
+    d2h = sum(8 << n for n, _ in circuits)
+    bufs = {n: hq.PinnedBuffer(1 << n) for n in set(n for n, _ in circuits)}
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        b2 = hq.Batch()
+        for c, s in zip(circs, states):
+            b2.add(c, s)
+        b2.compile()
+        b2.run()
+        for (n, _), s in zip(circuits, states):
+            s.store(bufs[n].array)
+        e2e.append(time.perf_counter() - t0)
+        b2.free()
+    for x in bufs.values():
+        x.free()
+    gates_total = sum(len(d) for _, d in circuits)
+    line = base_line(args, dist, f"batched circuits/s ({len(circuits)} circuits, n 10-22, depth 8-40)", value,
+                     "circuits/s", total_s * 1000 / args.steps, True,
+                     f"{len(circuits)} RY/RZ+CZ circuits, n uniform 10..22, depth uniform 8..40, one persistent "
+                     "launch (CUDA graph), states start at |0..0>",
+                     {"groups": info["groups"], "items": info["items"],
+                      "pass_bytes": info["pass_bytes"], "gates": gates_total,
+                      "tile_qubits_histogram": np.bincount(info["tile_qubits"]).tolist(),
+                      "compile_s": compile_s,
+                      "alone_device_ms": alone_dev / 1000.0, "alone_wall_ms": alone_wall * 1000.0,
+                      "speedup_vs_alone_wall": alone_wall / (total_s / args.steps),
+                      "max_abs_err_smallest8": max(errs), "max_norm_dev": norm_dev,
+                      "l2": "2.4 GB of states, larger than L2"})
+    line.update({"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                              "frac": achieved / peak, "traffic": None,
+                              "kernel": "k_oshm_batch<13,5>", "peak_source": peak_kind},
+                 "cpu_baseline": None,
+                 "e2e": {"value": dist.ws * len(circuits) * args.steps / dist.max(sum(e2e)),
+                         "unit": "circuits/s", "h2d_bytes_per_step": None,
+                         "d2h_bytes_per_step": int(d2h)},
+                 "gpu_launches": args.steps, "clocks": clk})
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_serve(args, dist: Dist):
+    """Config 5: Poisson streams through the request loop."""
+    import hyquas_gb300 as hq
+    from hyquas_gb300 import workloads as W
+    hq.init(dist.local)
+    count, nmax = args.serve_count, args.serve_nmax
+    rates = [200.0, 1000.0, 5000.0]
+    results = {}
+    base = W.served_stream(5 + dist.rank, count, 1000.0, 12, nmax)
+    arrays = [hq.gate_array(W.to_gates(d)) for _, _, d in base]
+    for rate in rates:
+        stream = W.served_stream(5 + dist.rank, count, rate, 12, nmax)
+        sv = hq.Server()
+        w = sv.submit(12, [])
+        sv.wait(w, 60)
+        sv.release(w)
+        sv.poll()
+        t0 = time.perf_counter()
+        times = {}
+        i = 0
+        while len(times) < count:
+            now = time.perf_counter() - t0
+            while i < count and stream[i][0] <= now:
+                sv.submit(stream[i][1], arrays[i])
+                i += 1
+            for rid in sv.poll():
+                if sv.wait(rid, 0) == "done":
+                    st = sv.state(rid)
+                    st.amps([0])
+                    st.sample(16, seed=rid)
+                times[rid] = sv.times(rid)
+                sv.release(rid)
+            time.sleep(0.0002)
+        lat = np.array([d - s for (s, a, d) in times.values()]) / 1e3
+        first = min(s for s, a, d in times.values())
+        last = max(d for s, a, d in times.values())
+        results[rate] = {"circuits_per_s": count / ((last - first) * 1e-6),
+                         "p50_ms": float(np.percentile(lat, 50)),
+                         "p99_ms": float(np.percentile(lat, 99)),
+                         "steps": sv.stats()["steps"],
+                         "peak_resident_gb": sv.stats()["peak_resident_bytes"] / 1e9}
+        sv.close()
+        if dist.rank == 0:
+            print(json.dumps({"serve_rate": rate, **results[rate]}), file=sys.stderr, flush=True)
+    # one at a time through the compiled path (same kernels): measured service times
+    serv = []
+    for (t, n, _), arr in zip(base, arrays):
+        a = time.perf_counter()
+        c = hq.Circuit(n)
+        c.addGates(arr)
+        c.compile("oshm", specialize=0)
+        s = hq.State(n)
+        c.run_on(s)
+        s.amps([0])
+        serv.append(time.perf_counter() - a)
+        s.free()
+    # plain gate-by-gate path: per-gate pass time measured at each qubit count
+    per_gate = {}
+    for n in sorted(set(n for _, n, _ in base)):
+        s = hq.State(n)
+        g = [hq.Gate.RY(q % n, 0.3) for q in range(8)]
+        s.apply_gates(g)
+        hq.synchronize()
+        a = time.perf_counter()
+        s.apply_gates(g)
+        hq.synchronize()
+        per_gate[n] = (time.perf_counter() - a) / len(g)
+        s.free()
+    plain = [len(d) * per_gate[n] for _, n, d in base]
+
+    def fifo(service, rate):
+        stream = W.served_stream(5 + dist.rank, count, rate, 12, nmax)
+        fin, lat = 0.0, []
+        for (t, _, _), sv_t in zip(stream, service):
+            fin = max(fin, t) + sv_t
+            lat.append(fin - t)
+        span = fin - stream[0][0]
+        return {"circuits_per_s": count / span, "p50_ms": float(np.percentile(lat, 50)) * 1e3,
+                "p99_ms": float(np.percentile(lat, 99)) * 1e3}
+
+    one = {r: fifo(serv, r) for r in rates}
+    plain_r = {r: fifo(plain, r) for r in rates}
+    head = results[1000.0]
+    line = base_line(args, dist, "served circuits/s at 1000/s arrivals (p50/p99 in config)",
+                     head["circuits_per_s"], "circuits/s", None, True,
+                     f"{count} Poisson requests per rate, n log-uniform 12..{nmax}, depth 10..60 "
+                     "RY/RZ+CZ; admission by 2^n x 8 B against 150 GB; results read (amplitude + "
+                     "16 samples) and released on completion",
+                     {"rates": {str(int(r)): results[r] for r in rates},
+                      "one_at_a_time_compiled": {str(int(r)): one[r] for r in rates},
+                      "one_at_a_time_plain_modelled": {str(int(r)): plain_r[r] for r in rates},
+                      "plain_model": "FIFO of gates x measured per-gate pass time at each n",
+                      "speedup_vs_plain": {str(int(r)): results[r]["circuits_per_s"] /
+                                           plain_r[r]["circuits_per_s"] for r in rates},
+                      "speedup_vs_compiled": {str(int(r)): results[r]["circuits_per_s"] /
+                                              one[r]["circuits_per_s"] for r in rates}})
+    line.update({"roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None})
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -310,6 +676,12 @@ def main():
     ap.add_argument("--grid", default="5x6", help="grid RxC of the circuit (5x6 = the 30-qubit "
                     "benchmark; smaller grids are for profiler captures)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="grid30",
+                    choices=["grid30", "plain20", "qft28", "batch", "serve"])
+    ap.add_argument("--qft-qubits", type=int, default=28)
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--serve-count", type=int, default=200)
+    ap.add_argument("--serve-nmax", type=int, default=32)
     args = ap.parse_args()
     args.grid = tuple(int(x) for x in args.grid.lower().split("x"))
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -317,8 +689,11 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, dist)
-        else:
+        elif args.workload == "grid30":
             run_ours(args, dist)
+        else:
+            {"plain20": run_plain20, "qft28": run_qft28, "batch": run_batch,
+             "serve": run_serve}[args.workload](args, dist)
     finally:
         dist.close()
 
