@@ -110,6 +110,7 @@ def _load():
         "hq_apply_transmm_group": [P, P, I32, U64, I32],
         "hq_apply_unitary": [P, P, U64, I32],
         "hq_group_unitary": [P, I32, U64, P],
+        "hq_qasm_parse": [C.c_char_p, C.POINTER(I32), P, I32, C.POINTER(I32)],
         "hq_server_options_default": [C.POINTER(hq_server_options)],
         "hq_server_check": [C.POINTER(hq_server_options), I32, P, I32],
         "hq_server_create": [C.POINTER(hq_server_options), C.POINTER(P)],
@@ -296,6 +297,17 @@ def gate_array(gates) -> C.Array:
     return arr
 
 
+def parse_qasm(text: str) -> tuple[int, list]:
+    """OpenQASM 2 text -> (num_qubits, [Gate]); the reference parser's subset
+    (main.cpp:12-230) plus u2, id, swap and skipped creg/barrier/measure."""
+    b = text.encode()
+    n, cnt = C.c_int32(), C.c_int32()
+    check(lib.hq_qasm_parse(b, C.byref(n), None, 0, C.byref(cnt)))
+    arr = (hq_gate * max(1, cnt.value))()
+    check(lib.hq_qasm_parse(b, C.byref(n), arr, cnt.value, C.byref(cnt)))
+    return n.value, [Gate(arr[i]) for i in range(cnt.value)]
+
+
 # --------------------------------------------------------------------------- state
 
 class State:
@@ -435,6 +447,14 @@ class Circuit:
         self.state: State | None = None
         self.result: np.ndarray | None = None
         self.gates: list[Gate] = []
+
+    @classmethod
+    def from_qasm(cls, text: str) -> "Circuit":
+        """parse_circuit, main.cpp:65-230."""
+        n, gates = parse_qasm(text)
+        c = cls(n)
+        c.addGates(gates)
+        return c
 
     @property
     def handle(self):
@@ -701,5 +721,5 @@ class Batch:
             pass
 
 
-__all__ = ["Circuit", "Batch", "Server", "Gate", "State", "ResultItem", "HQError", "init", "device_info",
+__all__ = ["Circuit", "Batch", "Server", "Gate", "State", "parse_qasm", "ResultItem", "HQError", "init", "device_info",
            "group_unitary", "set_hbm_budget", "hbm_in_use", "lib", "LIB_PATH"]

@@ -431,6 +431,25 @@ hq_status hq_circuit_capture_graph(hq_circuit c, hq_state s) {
     HQ_API_END
 }
 
+// ---- OpenQASM front-end --------------------------------------------------------------
+
+hq_status hq_qasm_parse(const char* text, int32_t* num_qubits, hq_gate* out, int32_t cap,
+                        int32_t* count) {
+    HQ_API_BEGIN
+    HQ_NONNULL(text);
+    int n = 0;
+    std::vector<hq_gate> gates;
+    parse_qasm(text, n, gates);
+    if (num_qubits) *num_qubits = n;
+    if (count) *count = (int32_t)gates.size();
+    if (out) {
+        HQ_REQUIRE(cap >= (int32_t)gates.size(), HQ_ERR_INVALID, "qasm: %zu gates, room for %d",
+                   gates.size(), cap);
+        std::copy(gates.begin(), gates.end(), out);
+    }
+    HQ_API_END
+}
+
 // ---- batches ------------------------------------------------------------------------
 
 hq_status hq_batch_create(hq_batch* out) {

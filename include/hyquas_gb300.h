@@ -95,6 +95,15 @@ hq_status hq_host_free(void* p);
 hq_status hq_gate_make(int32_t type, int32_t target, int32_t control, int32_t control2,
                        const double* params, hq_gate* out);
 
+/* Parse OpenQASM 2 text: the subset the reference's parser reads
+ * (parse_circuit, main.cpp:12-230: qreg; cx ccx cy cz h x y z s sdg t tdg;
+ * crx cry crz cu1 u1 u3 rx ry rz with pi*x / pi/x / decimal parameters),
+ * plus u2, id, swap, -pi*x / -pi/x, and skipped creg / barrier / measure.
+ * *num_qubits = the qreg size; the gates go to out[0..cap) and *count is
+ * their number (out may be NULL to ask for the count).  Errors name the line. */
+hq_status hq_qasm_parse(const char* text, int32_t* num_qubits, hq_gate* out, int32_t cap,
+                        int32_t* count);
+
 /* ---- state vector (src/kernelSimple.cu:9-37, 518-529) ------------------ */
 
 /* Allocate a 2^n complex64 state (no initialisation).  kernelInit's cudaMalloc,
