@@ -86,7 +86,89 @@ struct Amps {
     v2 re[NV], im[NV];
 };
 
+// ---- in-place register updates ----------------------------------------------
+// Every amplitude register is read and written through the same asm operand,
+// so each amplitude stays in one register through the op dispatch (no copies
+// where the dispatch's branches merge).
+
+// (l, h) <- (a l + b h, c l + d h), real coefficients (applied to re and im alike)
+__device__ __forceinline__ void ip_real(v2& l, v2& h, v2 a, v2 b, v2 c, v2 d) {
+    asm("{\n\t.reg .b64 t;\n\t"
+        "mul.rn.f32x2 t, %2, %0;\n\tfma.rn.f32x2 t, %3, %1, t;\n\t"
+        "mul.rn.f32x2 %1, %5, %1;\n\tfma.rn.f32x2 %1, %4, %0, %1;\n\t"
+        "mov.b64 %0, t;\n\t}"
+        : "+l"(l), "+l"(h) : "l"(a), "l"(b), "l"(c), "l"(d));
+}
+// (l, h) <- (l + h, l - h)
+__device__ __forceinline__ void ip_bfly(v2& l, v2& h) {
+    asm("{\n\t.reg .b64 t;\n\tadd.rn.f32x2 t, %0, %1;\n\tsub.rn.f32x2 %1, %0, %1;\n\tmov.b64 %0, t;\n\t}"
+        : "+l"(l), "+l"(h));
+}
+// (l, h) <- (l - h, l + h)
+__device__ __forceinline__ void ip_bfly_y(v2& l, v2& h) {
+    asm("{\n\t.reg .b64 t;\n\tsub.rn.f32x2 t, %0, %1;\n\tadd.rn.f32x2 %1, %0, %1;\n\tmov.b64 %0, t;\n\t}"
+        : "+l"(l), "+l"(h));
+}
+// sqrt(X) without its 1/sqrt2: (l, h) <- (l - i h, h - i l)
+__device__ __forceinline__ void ip_sx(v2& lr, v2& li, v2& hr, v2& hi) {
+    asm("{\n\t.reg .b64 a, b;\n\t"
+        "add.rn.f32x2 a, %0, %3;\n\tsub.rn.f32x2 b, %1, %2;\n\t"
+        "add.rn.f32x2 %2, %2, %1;\n\tsub.rn.f32x2 %3, %3, %0;\n\t"
+        "mov.b64 %0, a;\n\tmov.b64 %1, b;\n\t}"
+        : "+l"(lr), "+l"(li), "+l"(hr), "+l"(hi));
+}
+__device__ __forceinline__ void ip_swap(v2& l, v2& h) {
+    asm("{\n\t.reg .b64 t;\n\tmov.b64 t, %0;\n\tmov.b64 %0, %1;\n\tmov.b64 %1, t;\n\t}" : "+l"(l), "+l"(h));
+}
+// (r, i) <- (er r - ei i, ei r + er i); ein = -ei
+__device__ __forceinline__ void ip_cmul(v2& r, v2& i, v2 er, v2 ei, v2 ein) {
+    asm("{\n\t.reg .b64 t;\n\t"
+        "mul.rn.f32x2 t, %2, %0;\n\tfma.rn.f32x2 t, %4, %1, t;\n\t"
+        "mul.rn.f32x2 %1, %2, %1;\n\tfma.rn.f32x2 %1, %3, %0, %1;\n\t"
+        "mov.b64 %0, t;\n\t}"
+        : "+l"(r), "+l"(i) : "l"(er), "l"(ei), "l"(ein));
+}
+__device__ __forceinline__ void ip_scale(v2& x, v2 f) {
+    asm("mul.rn.f32x2 %0, %1, %0;" : "+l"(x) : "l"(f));
+}
+__device__ __forceinline__ void ip_xor(v2& x, v2 m) { asm("xor.b64 %0, %0, %1;" : "+l"(x) : "l"(m)); }
+// general complex 2x2: l' = a l + b h, h' = c l + d h (x = re, y = im, n = -im)
+__device__ __forceinline__ void ip_u(v2& lr, v2& li, v2& hr, v2& hi, const v2 (&k)[12]) {
+    asm("{\n\t.reg .b64 tr, ti, u;\n\t"
+        "mul.rn.f32x2 tr, %4, %0;\n\tfma.rn.f32x2 tr, %6, %1, tr;\n\t"
+        "fma.rn.f32x2 tr, %7, %2, tr;\n\tfma.rn.f32x2 tr, %9, %3, tr;\n\t"
+        "mul.rn.f32x2 ti, %4, %1;\n\tfma.rn.f32x2 ti, %5, %0, ti;\n\t"
+        "fma.rn.f32x2 ti, %7, %3, ti;\n\tfma.rn.f32x2 ti, %8, %2, ti;\n\t"
+        "mul.rn.f32x2 u, %13, %3;\n\tfma.rn.f32x2 u, %14, %2, u;\n\t"
+        "fma.rn.f32x2 u, %10, %1, u;\n\tfma.rn.f32x2 u, %11, %0, u;\n\t"
+        "mul.rn.f32x2 %2, %13, %2;\n\tfma.rn.f32x2 %2, %15, %3, %2;\n\t"
+        "fma.rn.f32x2 %2, %10, %0, %2;\n\tfma.rn.f32x2 %2, %12, %1, %2;\n\t"
+        "mov.b64 %3, u;\n\tmov.b64 %0, tr;\n\tmov.b64 %1, ti;\n\t}"
+        : "+l"(lr), "+l"(li), "+l"(hr), "+l"(hi)
+        : "l"(k[0]), "l"(k[1]), "l"(k[2]), "l"(k[3]), "l"(k[4]), "l"(k[5]), "l"(k[6]),
+          "l"(k[7]), "l"(k[8]), "l"(k[9]), "l"(k[10]), "l"(k[11]));
+}
+// [[a, i b], [i c, d]], real a..d: l' = a l + i b h, h' = i c l + d h
+__device__ __forceinline__ void ip_imoff(v2& lr, v2& li, v2& hr, v2& hi, v2 a, v2 b, v2 bn, v2 c,
+                                         v2 cn, v2 d) {
+    asm("{\n\t.reg .b64 tr, ti, u;\n\t"
+        "mul.rn.f32x2 tr, %4, %0;\n\tfma.rn.f32x2 tr, %6, %3, tr;\n\t"
+        "mul.rn.f32x2 ti, %4, %1;\n\tfma.rn.f32x2 ti, %5, %2, ti;\n\t"
+        "mul.rn.f32x2 u, %9, %3;\n\tfma.rn.f32x2 u, %7, %0, u;\n\t"
+        "mul.rn.f32x2 %2, %9, %2;\n\tfma.rn.f32x2 %2, %8, %1, %2;\n\t"
+        "mov.b64 %3, u;\n\tmov.b64 %0, tr;\n\tmov.b64 %1, ti;\n\t}"
+        : "+l"(lr), "+l"(li), "+l"(hr), "+l"(hi)
+        : "l"(a), "l"(b), "l"(bn), "l"(c), "l"(cn), "l"(d));
+}
+
 // ---- uncontrolled ops on register bit J >= 1 --------------------------------
+#define HQ_PAIRS_IP(J, NV, BODY)                           \
+    _Pragma("unroll") for (int j = 0; j < NV; j++) {        \
+        if (j & (1 << (J - 1))) continue;                    \
+        const int h = j | (1 << (J - 1));                    \
+        BODY                                                 \
+    }
+// read-only pair access for the register-controlled ops below
 #define HQ_PAIRS(J, NV, BODY)                              \
     _Pragma("unroll") for (int j = 0; j < NV; j++) {        \
         if (j & (1 << (J - 1))) continue;                    \
@@ -97,26 +179,17 @@ struct Amps {
 
 template <int J, int NV>
 __device__ __forceinline__ void op_u(Amps<NV>& A, const float (&m)[8]) {
-    const v2 a = vdup(m[0]), ai = vdup(m[1]), ain = vdup(-m[1]);
-    const v2 b = vdup(m[2]), bi = vdup(m[3]), bin = vdup(-m[3]);
-    const v2 c = vdup(m[4]), ci = vdup(m[5]), cin = vdup(-m[5]);
-    const v2 d = vdup(m[6]), di = vdup(m[7]), din = vdup(-m[7]);
-    HQ_PAIRS(J, NV, {
-        A.re[j] = vfma(bin, hi, vfma(b, hr, vfma(ain, li, vmul(a, lr))));
-        A.im[j] = vfma(bi, hr, vfma(b, hi, vfma(ai, lr, vmul(a, li))));
-        A.re[h] = vfma(din, hi, vfma(d, hr, vfma(cin, li, vmul(c, lr))));
-        A.im[h] = vfma(di, hr, vfma(d, hi, vfma(ci, lr, vmul(c, li))));
-    })
+    const v2 k[12] = {vdup(m[0]), vdup(m[1]), vdup(-m[1]), vdup(m[2]), vdup(m[3]), vdup(-m[3]),
+                      vdup(m[4]), vdup(m[5]), vdup(-m[5]), vdup(m[6]), vdup(m[7]), vdup(-m[7])};
+    HQ_PAIRS_IP(J, NV, { ip_u(A.re[j], A.im[j], A.re[h], A.im[h], k); })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_real(Amps<NV>& A, const float (&m)[8]) {
     const v2 a = vdup(m[0]), b = vdup(m[2]), c = vdup(m[4]), d = vdup(m[6]);
-    HQ_PAIRS(J, NV, {
-        A.re[j] = vfma(b, hr, vmul(a, lr));
-        A.im[j] = vfma(b, hi, vmul(a, li));
-        A.re[h] = vfma(d, hr, vmul(c, lr));
-        A.im[h] = vfma(d, hi, vmul(c, li));
+    HQ_PAIRS_IP(J, NV, {
+        ip_real(A.re[j], A.re[h], a, b, c, d);
+        ip_real(A.im[j], A.im[h], a, b, c, d);
     })
 }
 
@@ -125,51 +198,35 @@ template <int J, int NV>
 __device__ __forceinline__ void op_imoff(Amps<NV>& A, const float (&m)[8]) {
     const v2 a = vdup(m[0]), b = vdup(m[3]), bn = vdup(-m[3]), c = vdup(m[5]), cn = vdup(-m[5]),
              d = vdup(m[6]);
-    HQ_PAIRS(J, NV, {
-        A.re[j] = vfma(bn, hi, vmul(a, lr));
-        A.im[j] = vfma(b, hr, vmul(a, li));
-        A.re[h] = vfma(cn, li, vmul(d, hr));
-        A.im[h] = vfma(c, lr, vmul(d, hi));
-    })
+    HQ_PAIRS_IP(J, NV, { ip_imoff(A.re[j], A.im[j], A.re[h], A.im[h], a, b, bn, c, cn, d); })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_h(Amps<NV>& A) {
-    HQ_PAIRS(J, NV, {
-        A.re[j] = vadd(lr, hr);
-        A.im[j] = vadd(li, hi);
-        A.re[h] = vsub(lr, hr);
-        A.im[h] = vsub(li, hi);
+    HQ_PAIRS_IP(J, NV, {
+        ip_bfly(A.re[j], A.re[h]);
+        ip_bfly(A.im[j], A.im[h]);
     })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_sy(Amps<NV>& A) {
-    HQ_PAIRS(J, NV, {
-        A.re[j] = vsub(lr, hr);
-        A.im[j] = vsub(li, hi);
-        A.re[h] = vadd(lr, hr);
-        A.im[h] = vadd(li, hi);
+    HQ_PAIRS_IP(J, NV, {
+        ip_bfly_y(A.re[j], A.re[h]);
+        ip_bfly_y(A.im[j], A.im[h]);
     })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_sx(Amps<NV>& A) {
-    HQ_PAIRS(J, NV, {
-        A.re[j] = vadd(lr, hi);
-        A.im[j] = vsub(li, hr);
-        A.re[h] = vadd(hr, li);
-        A.im[h] = vsub(hi, lr);
-    })
+    HQ_PAIRS_IP(J, NV, { ip_sx(A.re[j], A.im[j], A.re[h], A.im[h]); })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_x(Amps<NV>& A) {
-    HQ_PAIRS(J, NV, {
-        A.re[j] = hr;
-        A.im[j] = hi;
-        A.re[h] = lr;
-        A.im[h] = li;
+    HQ_PAIRS_IP(J, NV, {
+        ip_swap(A.re[j], A.re[h]);
+        ip_swap(A.im[j], A.im[h]);
     })
 }
 
@@ -177,24 +234,18 @@ template <int J, int NV>
 __device__ __forceinline__ void op_dreg(Amps<NV>& A, const float (&m)[8], bool d0one) {
     const v2 er = vdup(m[6]), ei = vdup(m[7]), ein = vdup(-m[7]);
     const v2 fr = vdup(m[0]), fi = vdup(m[1]), fin = vdup(-m[1]);
-    HQ_PAIRS(J, NV, {
-        A.re[h] = vfma(ein, hi, vmul(er, hr));
-        A.im[h] = vfma(ei, hr, vmul(er, hi));
-        if (!d0one) {
-            A.re[j] = vfma(fin, li, vmul(fr, lr));
-            A.im[j] = vfma(fi, lr, vmul(fr, li));
-        }
+    HQ_PAIRS_IP(J, NV, {
+        ip_cmul(A.re[h], A.im[h], er, ei, ein);
+        if (!d0one) ip_cmul(A.re[j], A.im[j], fr, fi, fin);
     })
 }
 
 template <int J, int NV>
 __device__ __forceinline__ void op_neghi(Amps<NV>& A) {
-    const v2 n1 = vdup(-1.f);
-    HQ_PAIRS(J, NV, {
-        (void)lr;
-        (void)li;
-        A.re[h] = vmul(n1, hr);
-        A.im[h] = vmul(n1, hi);
+    const v2 sgn = 0x8000000080000000ull;
+    HQ_PAIRS_IP(J, NV, {
+        ip_xor(A.re[h], sgn);
+        ip_xor(A.im[h], sgn);
     })
 }
 
