@@ -212,6 +212,62 @@ uint64_t pad_tile(uint64_t mask, int k, int n) {
     return mask;
 }
 
+// Greedy grouping can leave a late group with a handful of gates, which then
+// costs a whole pass over the state.  Each gate of such a group moves to the
+// end of the latest earlier OShareMem group that can hold it -- its
+// non-diagonal target inside that group's tile (diagonal gates fit any tile)
+// -- provided every gate it moves past commutes with it (disjoint qubits, or
+// both diagonal).  The group is dropped when all of its gates found a place.
+void absorb_small_groups(Partition& part, const std::vector<hq_gate>& gates,
+                         const std::vector<char>& diag, int n, int max_gates) {
+    auto commute = [&](int a, int b) {
+        return (gate_qubits(gates[a]) & gate_qubits(gates[b])) == 0 || (diag[a] && diag[b]);
+    };
+    for (size_t g = part.groups.size(); g-- > 1;) {
+        const GroupPlan& src = part.groups[g];
+        if ((int)src.gates.size() > max_gates || src.backend != HQ_BACKEND_OSHM) continue;
+        std::vector<std::vector<int>> add(g);
+        std::vector<int> placed(src.gates.size(), -1);
+        bool ok = true;
+        for (size_t xi = 0; xi < src.gates.size() && ok; xi++) {
+            const int x = src.gates[xi];
+            int lb = 0;
+            for (size_t yi = 0; yi < xi; yi++)
+                if (!commute(src.gates[yi], x)) lb = std::max(lb, placed[yi]);
+            int where = -1;
+            for (int p = (int)g - 1; p >= lb; p--) {
+                const GroupPlan& gp = part.groups[p];
+                if (gp.backend == HQ_BACKEND_OSHM) {
+                    const uint64_t tile = pad_tile(gp.related | 1, gp.width, n);
+                    if (diag[x] || ((tile >> gates[x].target) & 1)) {
+                        where = p;
+                        break;
+                    }
+                }
+                bool pass = true;
+                for (int y : gp.gates) pass = pass && commute(y, x);
+                for (int y : add[p]) pass = pass && commute(y, x);
+                if (!pass) break;
+            }
+            if (where < 0) {
+                ok = false;
+                break;
+            }
+            placed[xi] = where;
+            add[where].push_back(x);
+        }
+        if (!ok) continue;
+        for (size_t p = 0; p < g; p++) {
+            GroupPlan& gp = part.groups[p];
+            for (int x : add[p]) {
+                gp.gates.push_back(x);
+                if (!diag[x]) gp.related |= uint64_t(1) << gates[x].target;
+            }
+        }
+        part.groups.erase(part.groups.begin() + g);
+    }
+}
+
 Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
                     const CompileConfig& cfg) {
     Partition out;
@@ -310,6 +366,7 @@ Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<
         out.groups.push_back(std::move(gp));
     }
     out.final_pos = pos;
+    if (!cfg.reference) absorb_small_groups(out, gates, in.diag, n, 16);
     return out;
 }
 

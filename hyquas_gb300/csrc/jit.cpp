@@ -362,12 +362,19 @@ std::string deposit_expr(const char* var, uint32_t nbits, const uint8_t* dst, bo
     return e.str();
 }
 
-std::string generate(const OshmProgram& prog, int& threads, size_t& smem) {
+// Two shapes of the same kernel.  PAIRED: two CTAs per SM, one tile buffer
+// each, registers capped at 128 so both fit; one CTA's tile load overlaps the
+// other's compute and the SM has 16 warps to hide latency.  SINGLE: one CTA per
+// SM that double-buffers its tiles; used when the paired build would spill.
+enum class Shape { PAIRED, SINGLE };
+
+std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape shape) {
+    const bool paired = shape == Shape::PAIRED;
     const int K = prog.k, R = prog.r, NV = 1 << (R - 1);
     const int T = 1 << (K - R);
     const int PPT = (1 << (K - 1)) / T;
     threads = T;
-    smem = 2 * (sizeof(float) * 2 << K);
+    smem = (paired ? 1 : 2) * (sizeof(float) * 2 << K);
     const int n = prog.n;
     uint8_t tile_phys[OSHM_MAX_K];
     for (int b = 0, j = 0; b < n; b++)
@@ -377,7 +384,7 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem) {
     g.nv = NV;
     std::ostringstream& o = g.o;
     o << kPrelude;
-    o << "extern \"C\" __global__ void __launch_bounds__(" << T
+    o << "extern \"C\" __global__ void __launch_bounds__(" << T << (paired ? ", 2" : "")
       << ") hq_oshm_group(float2* __restrict__ state, u64 ntiles) {\n";
     o << "extern __shared__ float4 smem4[];\nconst unsigned t = threadIdx.x;\n";
     // physical offset of local index 2t and its slot
@@ -429,15 +436,23 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem) {
         o << "const unsigned sb" << p << " = swz(" << deposit_expr("t", K - R, P.g_local, false) << ");\n";
         o << "const u64 gp" << p << " = " << deposit_expr("t", K - R, P.g_phys, true) << ";\n";
     }
-    o << "u64 u = blockIdx.x;\nif (u < ntiles) load_tile(u, 0);\n";
-    o << "for (int it = 0; u < ntiles; it++, u += gridDim.x) {\n"
-         "const u64 un = u + gridDim.x;\n"
-         "if (un < ntiles) { load_tile(un, (it + 1) & 1); asm volatile(\"cp.async.wait_group 1;\\n\" ::: "
-         "\"memory\"); }\n"
-         "else { asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\"); }\n"
-         "__syncthreads();\n"
-      << "float4* buf = smem4 + (it & 1) * " << (1 << (K - 1)) << ";\n"
-      << "const u64 base = tile_base(u);\n";
+    if (paired) {
+        o << "u64 u = blockIdx.x;\n";
+        o << "for (int it = 0; u < ntiles; it++, u += gridDim.x) {\n"
+             "load_tile(u, 0); asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\");\n"
+             "__syncthreads();\n"
+             "float4* buf = smem4;\n";
+    } else {
+        o << "u64 u = blockIdx.x;\nif (u < ntiles) load_tile(u, 0);\n";
+        o << "for (int it = 0; u < ntiles; it++, u += gridDim.x) {\n"
+             "const u64 un = u + gridDim.x;\n"
+             "if (un < ntiles) { load_tile(un, (it + 1) & 1); asm volatile(\"cp.async.wait_group 1;\\n\" ::: "
+             "\"memory\"); }\n"
+             "else { asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\"); }\n"
+             "__syncthreads();\n"
+          << "float4* buf = smem4 + (it & 1) * " << (1 << (K - 1)) << ";\n";
+    }
+    o << "const u64 base = tile_base(u);\n";
     o << "v2 ";
     for (int j = 0; j < NV; j++) o << (j ? ", " : "") << "r" << j << ", i" << j;
     o << ";\n";
@@ -544,6 +559,9 @@ JitKernel compile_source(const std::string& src, int threads, size_t smem) {
     k.smem = smem;
     HQ_CHECK_CUDA(cudaFuncSetAttribute((const void*)k.kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
+    cudaFuncAttributes fa;
+    HQ_CHECK_CUDA(cudaFuncGetAttributes(&fa, (const void*)k.kern));
+    k.local_bytes = fa.localSizeBytes;
     int bps = 0;
     HQ_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)k.kern, threads, smem));
     HQ_REQUIRE(bps >= 1, HQ_ERR_UNSUPPORTED, "specialised kernel does not fit on an SM");
@@ -560,7 +578,8 @@ std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>&
     std::vector<std::string> srcs(progs.size());
     std::vector<int> threads(progs.size());
     std::vector<size_t> smem(progs.size());
-    for (size_t i = 0; i < progs.size(); i++) srcs[i] = generate(*progs[i], threads[i], smem[i]);
+    for (size_t i = 0; i < progs.size(); i++)
+        srcs[i] = generate(*progs[i], threads[i], smem[i], Shape::PAIRED);
     std::vector<std::shared_ptr<CacheEntry>> ents(progs.size());
     std::vector<size_t> todo;
     {
@@ -594,7 +613,18 @@ std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>&
                     k = todo[next++];
                 }
                 try {
-                    ents[k]->k = compile_source(srcs[k], threads[k], smem[k]);
+                    JitKernel jk = compile_source(srcs[k], threads[k], smem[k]);
+                    // a spill of up to 128 bytes per thread costs less than the second
+                    // CTA gains (measured on the 30-qubit grid); beyond that, one
+                    // double-buffered CTA per SM
+                    if (jk.local_bytes > 128 || jk.blocks_per_sm < 2) {
+                        cudaLibraryUnload(jk.lib);
+                        int t2 = 0;
+                        size_t s2 = 0;
+                        const std::string src2 = generate(*progs[k], t2, s2, Shape::SINGLE);
+                        jk = compile_source(src2, t2, s2);
+                    }
+                    ents[k]->k = jk;
                     ents[k]->ok = true;
                 } catch (const Failure& f) {
                     ents[k]->err = f.what();
@@ -626,7 +656,7 @@ void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, cudaStream_t s
 std::string jit_source(const OshmProgram& prog) {
     int t;
     size_t s;
-    return generate(prog, t, s);
+    return generate(prog, t, s, Shape::PAIRED);
 }
 
 }  // namespace hq

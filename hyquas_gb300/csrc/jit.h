@@ -17,6 +17,7 @@ struct JitKernel {
     int threads = 0;
     size_t smem = 0;
     int blocks_per_sm = 1;
+    size_t local_bytes = 0;  // local memory per thread (register spills)
 };
 
 bool jit_available();
