@@ -430,12 +430,6 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
     for (int m = 0; m < PPT; m++)
         o << "cpa16(bb + ((tslot ^ " << pslot[m] << "u) << 3), gsrc + " << hex64(poff[m]) << ");\n";
     o << "asm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n};\n";
-    // per-phase thread constants (independent of the tile)
-    for (size_t p = 0; p < prog.phases.size(); p++) {
-        const OshmPhase& P = prog.phases[p];
-        o << "const unsigned sb" << p << " = swz(" << deposit_expr("t", K - R, P.g_local, false) << ");\n";
-        o << "const u64 gp" << p << " = " << deposit_expr("t", K - R, P.g_phys, true) << ";\n";
-    }
     if (paired) {
         o << "u64 u = blockIdx.x;\n";
         o << "for (int it = 0; u < ntiles; it++, u += gridDim.x) {\n"
@@ -458,7 +452,12 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
     o << ";\n";
     for (size_t p = 0; p < prog.phases.size(); p++) {
         const OshmPhase& P = prog.phases[p];
+        // the phase's thread constants, from an opaque copy of the thread index
+        // so that they are made here and not kept live across the whole kernel
         o << "{ // phase " << p << "\n";
+        o << "unsigned tp; asm volatile(\"mov.u32 %0, %1;\" : \"=r\"(tp) : \"r\"(t));\n";
+        o << "const unsigned sb" << p << " = swz(" << deposit_expr("tp", K - R, P.g_local, false) << ");\n";
+        o << "const u64 gp" << p << " = " << deposit_expr("tp", K - R, P.g_phys, true) << ";\n";
         o << "const u64 pidx = base | gp" << p << ";\n(void)pidx;\n";
         uint32_t col[OSHM_MAX_R];
         for (int j = 1; j < R; j++) col[j] = swz_host(1u << P.r_local[j]);
