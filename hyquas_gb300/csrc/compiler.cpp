@@ -2,6 +2,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstring>
 
 namespace hq {
@@ -402,6 +403,32 @@ int hadamard_like(const hq_gate& g) {
 
 }  // namespace
 
+namespace {
+
+// values within 1e-14 of 0 or +-1 are those exactly (so that RZ(pi) becomes a sign flip)
+double snap(double x) {
+    for (double v : {0.0, 1.0, -1.0})
+        if (std::fabs(x - v) < 1e-14) return v;
+    return x;
+}
+
+// the shear form of a rotation by phi: phi reduced to [-pi/2, pi/2] (a rotation
+// by pi is a negation), a = -tan(phi/2), b = sin(phi)
+void shear(double phi, OshmOp& o) {
+    const double pi = std::acos(-1.0);
+    if (phi > pi / 2) {
+        phi -= pi;
+        o.flags |= OPF_NEG;
+    } else if (phi < -pi / 2) {
+        phi += pi;
+        o.flags |= OPF_NEG;
+    }
+    o.m[0] = (float)(-std::tan(phi / 2));
+    o.m[1] = (float)std::sin(phi);
+}
+
+}  // namespace
+
 OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_mask) {
     OshmProgram prog;
     const int k = __builtin_popcountll(tile_mask);
@@ -430,6 +457,7 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
     }
 
     const double rsqrt2 = 1.0 / std::sqrt(2.0);
+    std::complex<double> gfac(1.0, 0.0);  // factors taken out of uncontrolled diagonal gates
     double pending_scale = 1.0;  // deferred 1/sqrt2 factors not applied yet
     int pending_count = 0;
     std::vector<char> done(gates.size(), 0);
@@ -534,12 +562,32 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
             const int lt = loc[g.target];
             const int rt = lt >= 0 ? reg_of_local[lt] : -1;
             if (diag[i]) {
-                const bool d0one = g.mat[0] == 1.0 && g.mat[1] == 0.0;
+                double d0r = g.mat[0], d0i = g.mat[1], d1r = g.mat[6], d1i = g.mat[7];
+                if (g.control < 0 && g.control2 < 0 && !(d0r == 1.0 && d0i == 0.0)) {
+                    // diag(d0, d1) = d0 diag(1, d1 / d0): d0 multiplies the whole state
+                    // and is applied once, at the end of the group
+                    const std::complex<double> d0(d0r, d0i), q = std::complex<double>(d1r, d1i) / d0;
+                    gfac *= d0;
+                    d0r = 1.0;
+                    d0i = 0.0;
+                    d1r = snap(q.real());
+                    d1i = snap(q.imag());
+                    o.m[0] = 1.f;
+                    o.m[1] = 0.f;
+                    o.m[6] = (float)d1r;
+                    o.m[7] = (float)d1i;
+                }
+                const bool d0one = d0r == 1.0 && d0i == 0.0;
                 if (d0one) o.flags |= OPF_D0_ONE;
-                if (d0one && g.mat[6] == 1.0 && g.mat[7] == 0.0) continue;  // identity
+                if (d0one && d1r == 1.0 && d1i == 0.0) continue;  // identity
                 if (rt >= 0) {
                     o.tbit = (uint8_t)rt;
-                    o.kind = (d0one && g.mat[6] == -1.0 && g.mat[7] == 0.0) ? OP_NEGHI : OP_DREG;
+                    o.kind = (d0one && d1r == -1.0 && d1i == 0.0) ? OP_NEGHI : OP_DREG;
+                    if (o.kind == OP_DREG && d0one && rt >= 1 && o.creg == 0 &&
+                        std::fabs(std::hypot(d1r, d1i) - 1.0) < 1e-12) {
+                        o.kind = OP_DROT;
+                        shear(std::atan2(d1i, d1r), o);
+                    }
                 } else {
                     o.kind = OP_DOUT;
                     o.tout = uint64_t(1) << g.target;
@@ -557,6 +605,8 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
                     pending_scale *= rsqrt2;
                     pending_count++;
                 } else if (rt >= 1 && o.creg == 0 && real) {
+                    // (OP_ROT, the shear form, measured slower here: its three
+                    // dependent FMAs per component cost more than a temporary)
                     o.kind = OP_REAL;
                 } else if (rt >= 1 && o.creg == 0 && imoff) {
                     o.kind = OP_IMOFF;
@@ -566,9 +616,19 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
             }
             prog.ops.push_back(o);
         }
-        ph.op_end = (uint32_t)prog.ops.size();
         for (int i : members) done[i] = 1;
         ndone += members.size();
+        if (ndone == gates.size() && gfac != std::complex<double>(1.0, 0.0)) {
+            // the factors taken out of diagonal gates, once, as a per-thread phase
+            OshmOp o;
+            std::memset(&o, 0, sizeof(o));
+            o.kind = OP_DOUT;
+            o.m[0] = o.m[6] = (float)gfac.real();
+            o.m[1] = o.m[7] = (float)gfac.imag();
+            prog.ops.push_back(o);
+            ph.flags |= PHF_ACC;
+        }
+        ph.op_end = (uint32_t)prog.ops.size();
         // apply the deferred factors before they could leave FP32 range
         // (2^(count/2) growth), and always at the last phase
         const bool last = ndone == gates.size();

@@ -266,10 +266,25 @@ struct Gen {
                 consts(nm, v, 6);
                 break;
             }
+            case OP_ROT:
+            case OP_DROT: {
+                const char* nm[] = {"sa", "sb"};
+                const float v[] = {m[0], m[1]};
+                consts(nm, v, 2);
+                break;
+            }
             case OP_NEGHI: break;
             default: break;
         }
         const bool d0one = (op.flags & OPF_D0_ONE) != 0;
+        const bool negf_op = (op.flags & OPF_NEG) != 0;
+        // in-place rotation of (x, y) by the three shears, then the optional negation
+        auto shear = [&](const std::string& x, const std::string& y, const char* x0, const char* y0) {
+            o << "{ v2 x = " << x0 << ", y = " << y0 << "; x = vfma(sa, y, x); y = vfma(sb, x, y); "
+              << "x = vfma(sa, y, x); ";
+            if (negf_op) o << "x ^= 0x8000000080000000ull; y ^= 0x8000000080000000ull; ";
+            o << x << " = x; " << y << " = y; }\n";
+        };
         for (int j = 0; j < nv; j++) {
             if (j & (1 << (J - 1))) continue;
             const int h = j | (1 << (J - 1));
@@ -328,6 +343,13 @@ struct Gen {
                         assign(R(j), "vfma(fin, li, vmul(fr, lr))", "lr", k0, k1);
                         assign(I(j), "vfma(fi, lr, vmul(fr, li))", "li", k0, k1);
                     }
+                    break;
+                case OP_ROT:
+                    shear(R(j), R(h), "lr", "hr");
+                    shear(I(j), I(h), "li", "hi");
+                    break;
+                case OP_DROT:
+                    shear(R(h), I(h), "hr", "hi");
                     break;
                 case OP_NEGHI: {
                     // sign flips as bit XORs: they run on the ALU pipe, not the FMA pipe

@@ -161,6 +161,12 @@ __device__ __forceinline__ void ip_imoff(v2& lr, v2& li, v2& hr, v2& hi, v2 a, v
         : "l"(a), "l"(b), "l"(bn), "l"(c), "l"(cn), "l"(d));
 }
 
+// rotation by the shears x += a y; y += b x; x += a y (a = -tan(phi/2), b = sin(phi))
+__device__ __forceinline__ void ip_shear(v2& x, v2& y, v2 a, v2 b) {
+    asm("fma.rn.f32x2 %0, %2, %1, %0;\n\tfma.rn.f32x2 %1, %3, %0, %1;\n\tfma.rn.f32x2 %0, %2, %1, %0;"
+        : "+l"(x), "+l"(y) : "l"(a), "l"(b));
+}
+
 // ---- uncontrolled ops on register bit J >= 1 --------------------------------
 #define HQ_PAIRS_IP(J, NV, BODY)                           \
     _Pragma("unroll") for (int j = 0; j < NV; j++) {        \
@@ -237,6 +243,33 @@ __device__ __forceinline__ void op_dreg(Amps<NV>& A, const float (&m)[8], bool d
     HQ_PAIRS_IP(J, NV, {
         ip_cmul(A.re[h], A.im[h], er, ei, ein);
         if (!d0one) ip_cmul(A.re[j], A.im[j], fr, fi, fin);
+    })
+}
+
+template <int J, int NV>
+__device__ __forceinline__ void op_rot(Amps<NV>& A, const float (&m)[8], bool neg) {
+    const v2 a = vdup(m[0]), b = vdup(m[1]), sgn = 0x8000000080000000ull;
+    HQ_PAIRS_IP(J, NV, {
+        ip_shear(A.re[j], A.re[h], a, b);
+        ip_shear(A.im[j], A.im[h], a, b);
+        if (neg) {
+            ip_xor(A.re[j], sgn);
+            ip_xor(A.im[j], sgn);
+            ip_xor(A.re[h], sgn);
+            ip_xor(A.im[h], sgn);
+        }
+    })
+}
+
+template <int J, int NV>
+__device__ __forceinline__ void op_drot(Amps<NV>& A, const float (&m)[8], bool neg) {
+    const v2 a = vdup(m[0]), b = vdup(m[1]), sgn = 0x8000000080000000ull;
+    HQ_PAIRS_IP(J, NV, {
+        ip_shear(A.re[h], A.im[h], a, b);
+        if (neg) {
+            ip_xor(A.re[h], sgn);
+            ip_xor(A.im[h], sgn);
+        }
     })
 }
 
@@ -424,6 +457,8 @@ __device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hd
         HQ_CASE_J(0, OP_X, (op_x<J, NV>(A)))
         HQ_CASE_J(0, OP_DREG, (op_dreg<J, NV>(A, m, d0one)))
         HQ_CASE_J(0, OP_NEGHI, (op_neghi<J, NV>(A)))
+        HQ_CASE_J(0, OP_ROT, (op_rot<J, NV>(A, m, (flags & OPF_NEG) != 0)))
+        HQ_CASE_J(0, OP_DROT, (op_drot<J, NV>(A, m, (flags & OPF_NEG) != 0)))
         HQ_CASE_J(1, OP_X, (ctl_x<J, NV>(A, creg)))
         HQ_CASE_J(1, OP_NEGHI, (ctl_diag<J, NV>(A, m, creg, true)))
         HQ_CASE_J(1, OP_DREG, (ctl_diag<J, NV>(A, m, creg, d0one)))
