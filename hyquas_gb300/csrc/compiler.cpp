@@ -605,8 +605,6 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
                     pending_scale *= rsqrt2;
                     pending_count++;
                 } else if (rt >= 1 && o.creg == 0 && real) {
-                    // (OP_ROT, the shear form, measured slower here: its three
-                    // dependent FMAs per component cost more than a temporary)
                     o.kind = OP_REAL;
                 } else if (rt >= 1 && o.creg == 0 && imoff) {
                     o.kind = OP_IMOFF;

@@ -266,7 +266,6 @@ struct Gen {
                 consts(nm, v, 6);
                 break;
             }
-            case OP_ROT:
             case OP_DROT: {
                 const char* nm[] = {"sa", "sb"};
                 const float v[] = {m[0], m[1]};
@@ -343,10 +342,6 @@ struct Gen {
                         assign(R(j), "vfma(fin, li, vmul(fr, lr))", "lr", k0, k1);
                         assign(I(j), "vfma(fi, lr, vmul(fr, li))", "li", k0, k1);
                     }
-                    break;
-                case OP_ROT:
-                    shear(R(j), R(h), "lr", "hr");
-                    shear(I(j), I(h), "li", "hi");
                     break;
                 case OP_DROT:
                     shear(R(h), I(h), "hr", "hi");

@@ -247,21 +247,6 @@ __device__ __forceinline__ void op_dreg(Amps<NV>& A, const float (&m)[8], bool d
 }
 
 template <int J, int NV>
-__device__ __forceinline__ void op_rot(Amps<NV>& A, const float (&m)[8], bool neg) {
-    const v2 a = vdup(m[0]), b = vdup(m[1]), sgn = 0x8000000080000000ull;
-    HQ_PAIRS_IP(J, NV, {
-        ip_shear(A.re[j], A.re[h], a, b);
-        ip_shear(A.im[j], A.im[h], a, b);
-        if (neg) {
-            ip_xor(A.re[j], sgn);
-            ip_xor(A.im[j], sgn);
-            ip_xor(A.re[h], sgn);
-            ip_xor(A.im[h], sgn);
-        }
-    })
-}
-
-template <int J, int NV>
 __device__ __forceinline__ void op_drot(Amps<NV>& A, const float (&m)[8], bool neg) {
     const v2 a = vdup(m[0]), b = vdup(m[1]), sgn = 0x8000000080000000ull;
     HQ_PAIRS_IP(J, NV, {
@@ -457,7 +442,6 @@ __device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hd
         HQ_CASE_J(0, OP_X, (op_x<J, NV>(A)))
         HQ_CASE_J(0, OP_DREG, (op_dreg<J, NV>(A, m, d0one)))
         HQ_CASE_J(0, OP_NEGHI, (op_neghi<J, NV>(A)))
-        HQ_CASE_J(0, OP_ROT, (op_rot<J, NV>(A, m, (flags & OPF_NEG) != 0)))
         HQ_CASE_J(0, OP_DROT, (op_drot<J, NV>(A, m, (flags & OPF_NEG) != 0)))
         HQ_CASE_J(1, OP_X, (ctl_x<J, NV>(A, creg)))
         HQ_CASE_J(1, OP_NEGHI, (ctl_diag<J, NV>(A, m, creg, true)))
