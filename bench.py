@@ -142,6 +142,14 @@ class Clocks:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
+def replica_throughput(dist: "Dist", units_per_rank: float, seconds: float):
+    """Whole-job throughput of N independent replicas: every rank did
+    `units_per_rank` units in `seconds`; the job takes the slowest rank's time.
+    Returns (units per second over all ranks, that time)."""
+    total_s = dist.max(seconds)
+    return dist.ws * units_per_rank / total_s, total_s
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -241,8 +249,7 @@ def run_ours(args, dist: Dist):
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
     dist.barrier()
-    total_s = dist.max(sum(dev_us) * 1e-6)
-    value = dist.ws * args.steps / total_s
+    value, total_s = replica_throughput(dist, args.steps, sum(dev_us) * 1e-6)
     ms_per_step = total_s * 1000.0 / args.steps
 
     # roofline of the dominant kernel (OShareMem): per-group CUDA-event times
@@ -355,8 +362,7 @@ def run_plain20(args, dist: Dist):
         dev.append(circ.run_on(state))
     clk = clocks.stop()
     dist.barrier()
-    total_s = dist.max(sum(dev) * 1e-6)
-    value = dist.ws * args.steps / total_s
+    value, total_s = replica_throughput(dist, args.steps, sum(dev) * 1e-6)
     ref = O.run_f64(n, desc)
     got = state.store()
     err = O.compare(ref, got)
@@ -504,8 +510,7 @@ def run_batch(args, dist: Dist):
     dev = [b.run() for _ in range(args.steps)]
     clk = clocks.stop()
     dist.barrier()
-    total_s = dist.max(sum(dev) * 1e-6)
-    value = dist.ws * len(circuits) * args.steps / total_s
+    value, total_s = replica_throughput(dist, len(circuits) * args.steps, sum(dev) * 1e-6)
     # correctness: the smallest circuits against the FP64 oracle, all norms
     order = sorted(range(len(circuits)), key=lambda i: circuits[i][0])
     errs = [O.compare(O.run_f64(*circuits[i]), states[i].store())["max_abs_err"] for i in order[:8]]
