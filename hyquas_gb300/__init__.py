@@ -131,6 +131,7 @@ def _load():
         "hq_batch_run": [P, I32, C.POINTER(D)],
         "hq_batch_enqueue": [P, I32],
         "hq_batch_capture_graph": [P, I32],
+        "hq_batch_inject_stall": [P],
         "hq_batch_info": [P, C.POINTER(I32), C.POINTER(I64), C.POINTER(I64), C.POINTER(U64), P],
     }
     for name, args in sig.items():
@@ -700,6 +701,10 @@ class Batch:
 
     def capture_graph(self, zero_init: bool = True):
         check(lib.hq_batch_capture_graph(self._h, 1 if zero_init else 0))
+
+    def inject_stall(self):
+        """Test hook: the next direct run's bounded device wait expires (HQ_ERR_TIMEOUT)."""
+        check(lib.hq_batch_inject_stall(self._h))
 
     def info(self) -> dict:
         nc, ng, ni, pb = C.c_int32(), C.c_int64(), C.c_int64(), C.c_uint64()

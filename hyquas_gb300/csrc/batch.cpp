@@ -155,6 +155,8 @@ void batch_compile(hq_batch_s* b, const hq_compile_options* opt) {
         }
     }
     b->num_items = items.size();
+    b->h_need.clear();
+    for (const BatchItem& it : items) b->h_need.push_back(it.need);
     HQ_REQUIRE(items.size() < (uint64_t(1) << 32) - 1, HQ_ERR_UNSUPPORTED, "batch: too many items");
 
     auto up16 = [](size_t x) { return (x + 255) & ~size_t(255); };
@@ -216,6 +218,18 @@ static void batch_enqueue_work(hq_batch_s* b, bool zero_init, cudaStream_t st) {
         HQ_CHECK_CUDA(cudaMemsetAsync(b->d_counters, 0, b->counters_bytes, st));
         BatchLaunch l = b->launch;
         l.zero_init = zero_init ? 1u : 0u;
+        l.stall_item = ~0u;
+        if (b->stall_next) {
+            // the first item that waits on a predecessor (else item 0) waits forever;
+            // its bounded wait gives up and the run reports HQ_ERR_TIMEOUT
+            l.stall_item = 0;
+            for (uint32_t i = 0; i < b->h_need.size(); i++)
+                if (b->h_need[i]) {
+                    l.stall_item = i;
+                    break;
+                }
+            b->stall_next = false;
+        }
         launch_oshm_batch(l, b->grid, b->cooperative, st);
     }
     for (BatchEntry& e : b->entries)
@@ -225,7 +239,7 @@ static void batch_enqueue_work(hq_batch_s* b, bool zero_init, cudaStream_t st) {
 void batch_enqueue(hq_batch_s* b, bool zero_init) {
     HQ_REQUIRE(b->compiled, HQ_ERR_STATE, "batch not compiled");
     cudaStream_t st = ctx().stream;
-    if (b->graph && b->graph_zero == zero_init) {
+    if (b->graph && b->graph_zero == zero_init && !b->stall_next) {
         for (BatchEntry& e : b->entries) {
             if (!zero_init) state_canonicalize(e.s);
         }

@@ -33,7 +33,9 @@ struct hq_batch_s {
     hq::BatchLaunch launch{};
     int grid = 0, slots = 0;
     bool cooperative = true;
+    bool stall_next = false;        // test hook: the next run's bounded wait expires
     int64_t num_groups = 0, num_items = 0;
+    std::vector<uint32_t> h_need;   // each item's dependency count (host copy)
     uint64_t pass_bytes = 0;
     cudaGraphExec_t graph = nullptr;
     bool graph_zero = false;

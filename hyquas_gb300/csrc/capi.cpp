@@ -510,6 +510,14 @@ hq_status hq_batch_enqueue(hq_batch b, int32_t zero_init) {
     HQ_API_END
 }
 
+hq_status hq_batch_inject_stall(hq_batch b) {
+    HQ_API_BEGIN
+    HQ_NONNULL(b);
+    HQ_REQUIRE(b->compiled, HQ_ERR_STATE, "batch not compiled");
+    b->stall_next = true;
+    HQ_API_END
+}
+
 hq_status hq_batch_capture_graph(hq_batch b, int32_t zero_init) {
     HQ_API_BEGIN
     HQ_NONNULL(b);

@@ -131,6 +131,7 @@ struct BatchLaunch {
     uint32_t* head;      // next item to hand out
     uint32_t* done;      // per circuit: tiles finished
     int* err;
+    uint32_t stall_item; // test hook: this item waits for a count never reached (~0u: none)
 };
 constexpr int kBatchTile = 13;  // widest tile of the batched kernel (2^13 amplitudes)
 constexpr int kBatchMinTile = 10;  // narrowest: one warp per tile

@@ -656,7 +656,8 @@ __global__ void __launch_bounds__(1 << (K - R)) k_oshm_batch(const BatchLaunch b
         const BatchItem it = b.items[i];
         if (t == 0) {
             bool ok = true;
-            if (it.need) ok = wait_counter(b.done + it.circuit, it.need, b.err, i);
+            const uint32_t need = i == b.stall_item ? 0xffffffffu : it.need;
+            if (need) ok = wait_counter(b.done + it.circuit, need, b.err, i);
             __threadfence();
             s_ok = ok;
         }

@@ -338,6 +338,7 @@ void enqueue_step(hq_server_s* sv, StepBuf& sb, std::vector<Request*>& newly,
         bl.head = ctr;
         bl.done = ctr + 1;
         bl.err = sv->d_err;
+        bl.stall_item = ~0u;
         const int grid = (int)std::min<size_t>(size_t(slots), std::max<size_t>(nitems, 1));
         launch_oshm_batch(bl, grid, true, st);
         HQ_CHECK_CUDA(cudaMemcpyAsync(sb.h_err, sv->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));

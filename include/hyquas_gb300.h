@@ -258,6 +258,11 @@ hq_status hq_batch_compile(hq_batch b, const hq_compile_options* opt);
 hq_status hq_batch_run(hq_batch b, int32_t zero_init, double* elapsed_us);
 /* Enqueue a run on the library stream without synchronising. */
 hq_status hq_batch_enqueue(hq_batch b, int32_t zero_init);
+/* Test hook for failure detection: the next direct run makes one work item
+ * wait for a completion count that is never reached.  The device-side wait is
+ * bounded (about 2 s); the run then returns HQ_ERR_TIMEOUT, and later runs
+ * work as before.  No GPU fault is involved. */
+hq_status hq_batch_inject_stall(hq_batch b);
 /* Capture a run into a CUDA graph; later runs with the same zero_init replay it. */
 hq_status hq_batch_capture_graph(hq_batch b, int32_t zero_init);
 /* num_circuits, total gate groups, work items and pass bytes (2 x 8 B x 2^n

@@ -143,3 +143,22 @@ def test_batch_config4_full(hq, oracle):
         alone = hq.State(n)
         c.run_on(alone)
         assert np.max(np.abs(alone.store().astype(np.complex128) - states[i].store())) <= 1e-6
+
+
+def test_batch_bounded_wait_reports_timeout(hq, oracle):
+    """Failure detection without a GPU fault: an item made to wait for a count
+    that is never reached gives up after its bounded wait; the run returns
+    HQ_ERR_TIMEOUT and the next run of the same batch is correct."""
+    import time
+    circuits = small_mix(seed=91, count=4, nmin=14, nmax=15, dmin=10, dmax=12)
+    b, states, _ = make_batch(hq, circuits)
+    assert b.info()["groups"] > len(circuits)  # some items wait on a predecessor
+    b.inject_stall()
+    t0 = time.time()
+    with pytest.raises(hq.HQError) as e:
+        b.run(zero_init=True)
+    assert e.value.code == -5  # HQ_ERR_TIMEOUT
+    assert time.time() - t0 < 30
+    b.run(zero_init=True)
+    for (n, desc), s in zip(circuits, states):
+        check(oracle, oracle.run_f64(n, desc), s.store())
