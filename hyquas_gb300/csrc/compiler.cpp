@@ -496,8 +496,10 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
             std::vector<int> score(k, 0);
             for (int i : members)
                 if (diag[i] && loc[gates[i].target] >= 0) score[loc[gates[i].target]]++;
+            // ties go to the highest tile qubits: the low ones stay thread bits, where
+            // they give whole 32-byte sectors to the stores of neighbouring threads
             std::vector<int> cand;
-            for (int b = 1; b < k; b++)
+            for (int b = k - 1; b >= 1; b--)
                 if (!((rset >> b) & 1)) cand.push_back(b);
             std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) { return score[a] < score[b]; });
             for (int b : cand) {

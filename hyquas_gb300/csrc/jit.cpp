@@ -447,7 +447,20 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
     for (int m = 0; m < PPT; m++)
         o << "cpa16(bb + ((tslot ^ " << pslot[m] << "u) << 3), gsrc + " << hex64(poff[m]) << ");\n";
     o << "asm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n};\n";
-    if (paired) {
+    // the last phase stores its amplitudes straight from registers to HBM, so
+    // the tile buffer is free once that phase has gathered them: a paired CTA
+    // then starts loading its next tile under the last phase's arithmetic
+    // Only when the last phase's first thread bit is physical qubit 1: then the
+    // 16-byte stores of neighbouring threads fill whole 32-byte sectors
+    // (otherwise the staged write-back through shared memory coalesces better).
+    const bool direct = !prog.phases.empty() && prog.phases.back().g_phys[0] == 1;
+    if (paired && direct) {
+        o << "u64 u = blockIdx.x;\nif (u < ntiles) load_tile(u, 0);\n";
+        o << "for (int it = 0; u < ntiles; it++, u += gridDim.x) {\n"
+             "asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\");\n"
+             "__syncthreads();\n"
+             "float4* buf = smem4;\n";
+    } else if (paired) {
         o << "u64 u = blockIdx.x;\n";
         o << "for (int it = 0; u < ntiles; it++, u += gridDim.x) {\n"
              "load_tile(u, 0); asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\");\n"
@@ -469,6 +482,7 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
     o << ";\n";
     for (size_t p = 0; p < prog.phases.size(); p++) {
         const OshmPhase& P = prog.phases[p];
+        const bool lastp = direct && p + 1 == prog.phases.size();
         // the phase's thread constants, from an opaque copy of the thread index
         // so that they are made here and not kept live across the whole kernel
         o << "{ // phase " << p << "\n";
@@ -488,6 +502,10 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
             else
                 o << "{ const ulonglong2 q = ((const ulonglong2*)buf)[(sb" << p << " ^ " << c
                   << "u) >> 1]; r" << j << " = q.x; i" << j << " = q.y; }\n";
+        }
+        if (lastp) {
+            o << "__syncthreads();\n";  // every amplitude is in registers: the buffer is free
+            if (paired) o << "if (u + gridDim.x < ntiles) load_tile(u + gridDim.x, 0);\n";
         }
         o << "float2 acc = make_float2(1.f, 0.f);\n(void)acc;\nbool negf = false;\n(void)negf;\n";
         bool uses_acc = false;
@@ -516,6 +534,18 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
             }
             o << "}\n";
         }
+        if (lastp) {
+            // vector j holds the amplitudes at pidx | (its register bits) and + 1
+            for (int j = 0; j < NV; j++) {
+                uint64_t off = 0;
+                for (int b = 1; b < R; b++)
+                    if ((j >> (b - 1)) & 1) off |= uint64_t(1) << tile_phys[P.r_local[b]];
+                o << "{ float4 w; vunpack(r" << j << ", w.x, w.z); vunpack(i" << j
+                  << ", w.y, w.w); *(float4*)(state + (pidx | " << hex64(off) << ")) = w; }\n";
+            }
+            o << "}\n";
+            continue;
+        }
         for (int j = 0; j < NV; j++) {
             uint32_t c = 0;
             for (int b = 1; b < R; b++)
@@ -525,16 +555,23 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
         }
         o << "__syncthreads();\n}\n";
     }
-    // write back in place; pieces are (re0, re1, im0, im1) after a phase
-    o << "float2* gdst = state + base + toff;\n";
-    for (int m = 0; m < PPT && prog.phases.empty(); m++)
-        o << "*(float4*)(gdst + " << hex64(poff[m]) << ") = buf[(tslot ^ " << pslot[m] << "u) >> 1];\n";
-    for (int m = 0; m < PPT && !prog.phases.empty(); m++) {
-        o << "{ const ulonglong2 q = ((const ulonglong2*)buf)[(tslot ^ " << pslot[m]
-          << "u) >> 1]; float4 w; vunpack(q.x, w.x, w.z); vunpack(q.y, w.y, w.w); *(float4*)(gdst + "
-          << hex64(poff[m]) << ") = w; }\n";
+    if (!direct) {
+        // staged write-back; pieces are (re0, re1, im0, im1) after a phase and
+        // as loaded when there is none
+        o << "float2* gdst = state + base + toff;\n";
+        for (int m = 0; m < PPT; m++) {
+            if (prog.phases.empty())
+                o << "*(float4*)(gdst + " << hex64(poff[m]) << ") = buf[(tslot ^ " << pslot[m]
+                  << "u) >> 1];\n";
+            else
+                o << "{ const ulonglong2 q = ((const ulonglong2*)buf)[(tslot ^ " << pslot[m]
+                  << "u) >> 1]; float4 w; vunpack(q.x, w.x, w.z); vunpack(q.y, w.y, w.w); "
+                     "*(float4*)(gdst + "
+                  << hex64(poff[m]) << ") = w; }\n";
+        }
+        o << "__syncthreads();\n";
     }
-    o << "__syncthreads();\n}\n}\n";
+    o << "}\n}\n";
     return o.str();
 }
 
