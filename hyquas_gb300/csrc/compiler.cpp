@@ -701,8 +701,8 @@ static const double kPassFloor = 2.4e-12;       // s per amplitude: 16 B at 6.7 
 static const double kOshmGate = 6.6e-14;        // s per amplitude per non-diagonal gate
 static const double kOshmDiag = 0.3 * 6.6e-14;  // uncontrolled diagonal gate
 static const double kOshmCtrlDiag = 1.4 * 6.6e-14;  // controlled diagonal gate
-static const double kMmBf16x3 = 7.8e-12;        // s per amplitude per 6-qubit TransMM pass
-static const double kMmTf32 = 6.6e-12;
+static const double kMmBf16x3 = 5.4e-12;        // s per amplitude per 6-qubit TransMM pass
+static const double kMmTf32 = 4.6e-12;
 static const double kMmFp32 = 1.5e-11;
 static const double kLaunchSec = 4e-6;
 

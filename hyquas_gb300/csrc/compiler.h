@@ -44,8 +44,8 @@ struct Partition {
 Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
                     const CompileConfig& cfg);
 
-// GB300 cost model (seconds) used by the hybrid backend; refitted constants
-// live in costmodel.cpp.
+// GB300 cost model (seconds) used by the hybrid backend; the constants are
+// fitted to kernel timings on GB300 (compiler.cpp).
 double cost_oshm(int n, int nphases, const std::vector<hq_gate>& gates, int k);
 double cost_transmm(int n, int m, int precision);
 

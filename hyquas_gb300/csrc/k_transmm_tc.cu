@@ -2,9 +2,9 @@
 //
 // A group of m = 6 qubits fused into a 64x64 complex unitary U is applied to
 // every tile of 2^13 amplitudes gathered in place (rows = the group's qubits,
-// columns = 128 other qubits), as the real-form GEMM
+// columns = 128 other qubits), each half of 64 columns as the real-form GEMM
 //
-//     [Cr; Ci] (128 x 128) = [[Ur, -Ui], [Ui, Ur]] (128 x 128) . [Br; Bi] (128 x 128)
+//     [Cr; Ci] (128 x 64) = [[Ur, -Ui], [Ui, Ur]] (128 x 128) . [Br; Bi] (128 x 64)
 //
 // on the 5th-generation tensor cores: operands in shared memory (K-major,
 // canonical 8x16-byte core matrices, no swizzle), the FP32 accumulator in
@@ -28,17 +28,19 @@ namespace hq {
 
 namespace {
 
-constexpr int TC_THREADS = 128;
+constexpr int TC_THREADS = 256;
 constexpr int TC_TILE_BITS = 13;
-constexpr int TC_ROWS = 64;      // 2^m, m = 6
-constexpr int TC_COLS = 128;     // 2^(13 - m)
-constexpr uint32_t SM_T = 0;           // tile, float2[8192]
-constexpr uint32_t SM_A = 65536;       // A operand, 64 KB
-constexpr uint32_t SM_B = 131072;      // B operand, 64 KB
-constexpr uint32_t SM_MISC = 196608;   // mbarrier, TMEM slot, row/column slot tables
+constexpr int TC_ROWS = 64;       // 2^m, m = 6
+constexpr int TC_NSUB = 64;       // columns of a sub-tile (half of the tile's 128)
+constexpr uint32_t SUB_BYTES = 32768;  // a sub-tile, float2[4096]
+constexpr uint32_t SM_A = 0;           // A operand, 64 KB
+constexpr uint32_t SM_B = 65536;       // B operand, two buffers of 32 KB
+constexpr uint32_t SM_R = 131072;      // sub-tile staging, three buffers of 32 KB
+constexpr uint32_t SM_MISC = 229376;   // mbarriers, TMEM slot, row/column slot tables
 constexpr uint32_t SM_TOTAL = SM_MISC + 1024;
-constexpr uint32_t TMEM_COLS = 128;
+constexpr uint32_t TMEM_COLS = 128;    // two accumulators of 64 columns
 constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier polls (with nanosleep)
+static_assert(SM_TOTAL <= 232448, "shared memory per block");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -124,15 +126,18 @@ __host__ __device__ __forceinline__ uint32_t kmajor_off(uint32_t row, uint32_t k
     return (row / 8) * sbo + (k / per_core) * 128 + (row % 8) * 16 + (k % per_core) * esize;
 }
 
+// One CTA per SM runs a pipeline over its sub-tiles j (64 rows x 64 columns):
+//   load j+2 (cp.async) | convert j -> B[j&1], MMA j -> TMEM acc[j&1] | epilogue j-1
+// Sub-tile j is staged in R[j%3]; its results are written back over it (the
+// raw amplitudes are dead once converted) and stored to HBM from there.
 template <int PREC>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunch p) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    float2* T = reinterpret_cast<float2*>(smem + SM_T);
     uint32_t* rowslot = reinterpret_cast<uint32_t*>(smem + SM_MISC + 64);
     uint32_t* colslot = rowslot + TC_ROWS;
     const uint32_t sb = smem_u32(smem);
-    const uint32_t s_mbar = sb + SM_MISC;
-    const uint32_t s_tslot = sb + SM_MISC + 8;
+    const uint32_t s_mbar = sb + SM_MISC;         // two mbarriers, 8 bytes each
+    const uint32_t s_tslot = sb + SM_MISC + 16;
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     float2* __restrict__ state = reinterpret_cast<float2*>(p.state);
 
@@ -143,18 +148,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
     }
     if (t == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar + 8));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     for (int r = t; r < TC_ROWS; r += TC_THREADS) {
         uint32_t x = 0;
         for (int b = 0; b < 6; b++)
-            if ((r >> b) & 1) x |= 1u << p.row_local[b];
+            if ((r >> b) & 1) x |= 1u << p.row_sub[b];
         rowslot[r] = tile_swz(x);
     }
-    for (int c = t; c < TC_COLS; c += TC_THREADS) {
+    for (int c = t; c < TC_NSUB; c += TC_THREADS) {
         uint32_t x = 0;
-        for (int b = 0; b < 7; b++)
-            if ((c >> b) & 1) x |= 1u << p.col_local[b];
+        for (int b = 0; b < 6; b++)
+            if ((c >> b) & 1) x |= 1u << p.col_sub[b];
         colslot[c] = tile_swz(x);
     }
     // the group's A operand (prepared once per circuit), 64 KB
@@ -166,47 +172,98 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + SM_MISC + 8);
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + SM_MISC + 16);
 
-    const uint64_t toff = local_to_phys(uint32_t(t) << 1, TC_TILE_BITS, p.tile_phys);
+    const uint64_t toff = local_to_phys(uint32_t(t) << 1, TC_TILE_BITS - 1, p.sub_phys);
     const uint32_t tsl = tile_swz(uint32_t(t) << 1);
     constexpr uint32_t esize = PREC == HQ_MM_TF32 ? 4 : 2;
     constexpr uint32_t kstep_bytes = 256;  // 16 bf16 or 8 tf32 K-elements = two core matrices
     constexpr uint32_t sbo = (128 / (16 / esize)) * 128;
-    constexpr uint32_t idesc = make_idesc(PREC == HQ_MM_TF32 ? 2u : 1u, 128, 128);
-    const int nsteps = PREC == HQ_MM_TF32 ? 16 : 8;
+    constexpr uint32_t b_lo = 16384;       // B lo half (BF16x3): 64 rows x 128 K bf16
+    constexpr uint32_t idesc = make_idesc(PREC == HQ_MM_TF32 ? 2u : 1u, 128, TC_NSUB);
+    constexpr int nsteps = PREC == HQ_MM_TF32 ? 16 : 8;
 
-    int it = 0;
-    for (uint64_t u = blockIdx.x; u < p.ntiles; u += gridDim.x, it++) {
-        const uint64_t base = tile_base(u, p.nruns, p.run_src, p.run_dst, p.run_len);
-        const float2* gsrc = state + base + toff;
-#pragma unroll 8
-        for (int m = 0; m < 32; m++)
-            cp_async16(sb + SM_T + (tsl ^ p.piece_slot128[m]) * 8u, gsrc + p.piece_off128[m]);
+    const uint64_t nsub = p.ntiles * 2;
+    const uint64_t G = gridDim.x;
+    const uint64_t J = blockIdx.x < nsub ? (nsub - blockIdx.x + G - 1) / G : 0;
+    auto sub_base = [&](uint64_t j) {
+        const uint64_t v = blockIdx.x + j * G;
+        return tile_base(v >> 1, p.nruns, p.run_src, p.run_dst, p.run_len) + (v & 1) * p.split_off;
+    };
+    auto load = [&](uint64_t j) {
+        if (j < J) {
+            const float2* gsrc = state + sub_base(j) + toff;
+            const uint32_t rb = sb + SM_R + uint32_t(j % 3) * SUB_BYTES;
+#pragma unroll
+            for (int m = 0; m < 8; m++)
+                cp_async16(rb + (tsl ^ p.sub_piece_slot[m]) * 8u, gsrc + p.sub_piece_off[m]);
+        }
         cp_async_commit();
-        cp_async_wait_all();
-        __syncthreads();
-
-        // B operand: column n = t; K index k = component * 64 + row
+    };
+    // results of sub-tile j: TMEM acc[j&1] -> over its staging buffer -> HBM
+    bool failed = false;
+    auto epilogue = [&](uint64_t j) {
+        const uint32_t b = uint32_t(j & 1);
+        const bool ok = mbar_wait(s_mbar + 8 * b, uint32_t((j >> 1) & 1));
+        if (__syncthreads_or(!ok)) {
+            if (t == 0 && p.err) {
+                atomicCAS(p.err, 0, 1);
+                p.err[1] = 7;  // site: TransMM accumulator wait
+                p.err[2] = (int)(j & 0x7fffffff);
+            }
+            failed = true;
+            return;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        // D row i = TMEM lane i: i < 64 the real part of row i, else the imaginary part of row i-64
+        float* Rf = reinterpret_cast<float*>(smem + SM_R + uint32_t(j % 3) * SUB_BYTES);
         {
-            const uint32_t cs = colslot[t];
-            for (int rb = 0; rb < 8; rb++) {
+            const int q = warp & 3, half = warp >> 2;
+            const int i = 32 * q + lane;
+            const uint32_t rs = rowslot[i & 63], comp = uint32_t(i >> 6);
+            uint32_t v[32];
+            tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + b * TC_NSUB + 32 * half, v);
+#pragma unroll
+            for (int c = 0; c < 32; c++) Rf[2 * (rs ^ colslot[32 * half + c]) + comp] = __uint_as_float(v[c]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        float2* gdst = state + sub_base(j) + toff;
+        const float4* R4 = reinterpret_cast<const float4*>(Rf);
+#pragma unroll
+        for (int m = 0; m < 8; m++)
+            *reinterpret_cast<float4*>(gdst + p.sub_piece_off[m]) = R4[(tsl ^ p.sub_piece_slot[m]) >> 1];
+        __syncthreads();
+    };
+
+    load(0);
+    load(1);
+    for (uint64_t j = 0; j < J && !failed; j++) {
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncthreads();
+        // B operand of sub-tile j: column n; K index k = component * 64 + row
+        {
+            const float2* Rj = reinterpret_cast<const float2*>(smem + SM_R + uint32_t(j % 3) * SUB_BYTES);
+            unsigned char* B = smem + SM_B + uint32_t(j & 1) * 32768u;
+            const int n = t & 63;
+            const uint32_t cs = colslot[n];
+            for (int rb = 2 * (t >> 6); rb < 2 * (t >> 6) + 2; rb++) {
                 float re[8], im[8];
 #pragma unroll
                 for (int q = 0; q < 8; q++) {
-                    const float2 a = T[rowslot[rb * 8 + q] ^ cs];
+                    const float2 a = Rj[rowslot[rb * 8 + q] ^ cs];
                     re[q] = a.x;
                     im[q] = a.y;
                 }
                 if (PREC == HQ_MM_TF32) {
 #pragma unroll
                     for (int half = 0; half < 2; half++) {
-                        const uint32_t ore = kmajor_off(t, rb * 8 + half * 4, 128, 4);
-                        const uint32_t oim = kmajor_off(t, 64 + rb * 8 + half * 4, 128, 4);
-                        *reinterpret_cast<float4*>(smem + SM_B + ore) =
+                        const uint32_t ore = kmajor_off(n, rb * 8 + half * 4, 128, 4);
+                        const uint32_t oim = kmajor_off(n, 64 + rb * 8 + half * 4, 128, 4);
+                        *reinterpret_cast<float4*>(B + ore) =
                             make_float4(to_tf32(re[4 * half]), to_tf32(re[4 * half + 1]),
                                         to_tf32(re[4 * half + 2]), to_tf32(re[4 * half + 3]));
-                        *reinterpret_cast<float4*>(smem + SM_B + oim) =
+                        *reinterpret_cast<float4*>(B + oim) =
                             make_float4(to_tf32(im[4 * half]), to_tf32(im[4 * half + 1]),
                                         to_tf32(im[4 * half + 2]), to_tf32(im[4 * half + 3]));
                     }
@@ -229,14 +286,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
                         him[q] = pack_bf16(g0, g1);
                         lim[q] = pack_bf16(k0, k1);
                     }
-                    const uint32_t ore = kmajor_off(t, rb * 8, 128, 2);
-                    const uint32_t oim = kmajor_off(t, 64 + rb * 8, 128, 2);
-                    *reinterpret_cast<uint4*>(smem + SM_B + ore) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
-                    *reinterpret_cast<uint4*>(smem + SM_B + oim) = make_uint4(him[0], him[1], him[2], him[3]);
-                    *reinterpret_cast<uint4*>(smem + SM_B + 32768 + ore) =
-                        make_uint4(lre[0], lre[1], lre[2], lre[3]);
-                    *reinterpret_cast<uint4*>(smem + SM_B + 32768 + oim) =
-                        make_uint4(lim[0], lim[1], lim[2], lim[3]);
+                    const uint32_t ore = kmajor_off(n, rb * 8, 128, 2);
+                    const uint32_t oim = kmajor_off(n, 64 + rb * 8, 128, 2);
+                    *reinterpret_cast<uint4*>(B + ore) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+                    *reinterpret_cast<uint4*>(B + oim) = make_uint4(him[0], him[1], him[2], him[3]);
+                    *reinterpret_cast<uint4*>(B + b_lo + ore) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
+                    *reinterpret_cast<uint4*>(B + b_lo + oim) = make_uint4(lim[0], lim[1], lim[2], lim[3]);
                 }
             }
         }
@@ -246,62 +301,34 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
 
         if (t == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t d = tmem + uint32_t(j & 1) * TC_NSUB;
+            const uint32_t bsm = sb + SM_B + uint32_t(j & 1) * 32768u;
             if (PREC == HQ_MM_TF32) {
                 for (int kk = 0; kk < nsteps; kk++)
-                    mma_tf32(tmem, make_desc(sb + SM_A + kk * kstep_bytes, 128, sbo),
-                             make_desc(sb + SM_B + kk * kstep_bytes, 128, sbo), idesc, kk > 0);
+                    mma_tf32(d, make_desc(sb + SM_A + kk * kstep_bytes, 128, sbo),
+                             make_desc(bsm + kk * kstep_bytes, 128, sbo), idesc, kk > 0);
             } else {
                 for (int kk = 0; kk < nsteps; kk++)  // hi . hi
-                    mma_f16(tmem, make_desc(sb + SM_A + kk * kstep_bytes, 128, sbo),
-                            make_desc(sb + SM_B + kk * kstep_bytes, 128, sbo), idesc, kk > 0);
+                    mma_f16(d, make_desc(sb + SM_A + kk * kstep_bytes, 128, sbo),
+                            make_desc(bsm + kk * kstep_bytes, 128, sbo), idesc, kk > 0);
                 for (int kk = 0; kk < nsteps; kk++)  // hi . lo
-                    mma_f16(tmem, make_desc(sb + SM_A + kk * kstep_bytes, 128, sbo),
-                            make_desc(sb + SM_B + 32768 + kk * kstep_bytes, 128, sbo), idesc, 1);
+                    mma_f16(d, make_desc(sb + SM_A + kk * kstep_bytes, 128, sbo),
+                            make_desc(bsm + b_lo + kk * kstep_bytes, 128, sbo), idesc, 1);
                 for (int kk = 0; kk < nsteps; kk++)  // lo . hi
-                    mma_f16(tmem, make_desc(sb + SM_A + 32768 + kk * kstep_bytes, 128, sbo),
-                            make_desc(sb + SM_B + kk * kstep_bytes, 128, sbo), idesc, 1);
+                    mma_f16(d, make_desc(sb + SM_A + 32768 + kk * kstep_bytes, 128, sbo),
+                            make_desc(bsm + kk * kstep_bytes, 128, sbo), idesc, 1);
             }
             asm volatile(
                 "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                    s_mbar)
+                    s_mbar + 8 * uint32_t(j & 1))
                 : "memory");
         }
-        const bool ok = mbar_wait(s_mbar, uint32_t(it & 1));
-        if (__syncthreads_or(!ok)) {
-            if (t == 0 && p.err) {
-                atomicCAS(p.err, 0, 1);
-                p.err[1] = 7;  // site: TransMM accumulator wait
-                p.err[2] = (int)(u & 0x7fffffff);
-            }
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-
-        // D row i (TMEM lane i): i < 64 -> real part of row i, else imaginary of row i-64
-        {
-            const int i = 32 * warp + lane;
-            const uint32_t rs = rowslot[i & 63];
-            float* Tf = reinterpret_cast<float*>(T);
-            const uint32_t comp = uint32_t(i >> 6);
-#pragma unroll 1
-            for (int c = 0; c < 4; c++) {
-                uint32_t v[32];
-                tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 32 * c, v);
-#pragma unroll
-                for (int q = 0; q < 32; q++)
-                    Tf[2 * (rs ^ colslot[32 * c + q]) + comp] = __uint_as_float(v[q]);
-            }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
-
-        float2* gdst = state + base + toff;
-#pragma unroll 8
-        for (int m = 0; m < 32; m++)
-            *reinterpret_cast<float4*>(gdst + p.piece_off128[m]) =
-                reinterpret_cast<const float4*>(T)[(tsl ^ p.piece_slot128[m]) >> 1];
-        __syncthreads();
+        if (j > 0) epilogue(j - 1);
+        if (failed) break;
+        load(j + 2);  // into R[(j+2)%3], the buffer sub-tile j-1 just left
     }
+    if (!failed && J > 0) epilogue(J - 1);
+    cp_async_wait_all();
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));

@@ -271,13 +271,26 @@ static TransmmLaunch make_launch(int n, int m, uint64_t rows, uint64_t tile, int
         p.piece_off[mm] = off;
         p.piece_slot[mm] = tile_swz(local);
     }
-    for (int mm = 0; mm < 32; mm++) {
-        const uint32_t local = uint32_t(2 * mm * 128);
-        uint64_t off = 0;
-        for (int j = 0; j < kSimtK; j++)
-            if ((local >> j) & 1) off |= uint64_t(1) << p.tile_phys[j];
-        p.piece_off128[mm] = off;
-        p.piece_slot128[mm] = tile_swz(local);
+    // sub-tiles for the tensor-core kernel (6 row bits + 7 column bits): the top
+    // column bit splits the tile
+    if (m == 6) {
+        const int split = p.col_local[6];
+        int sub[16];
+        for (int j = 0, q = 0; j < kSimtK; j++) {
+            sub[j] = j == split ? -1 : q;
+            if (j != split) p.sub_phys[q++] = p.tile_phys[j];
+        }
+        for (int r = 0; r < 6; r++) p.row_sub[r] = (uint8_t)sub[p.row_local[r]];
+        for (int c = 0; c < 6; c++) p.col_sub[c] = (uint8_t)sub[p.col_local[c]];
+        p.split_off = uint64_t(1) << p.tile_phys[split];
+        for (int mm = 0; mm < 8; mm++) {
+            const uint32_t local = uint32_t(2 * mm * 256);
+            uint64_t off = 0;
+            for (int j = 0; j < kSimtK - 1; j++)
+                if ((local >> j) & 1) off |= uint64_t(1) << p.sub_phys[j];
+            p.sub_piece_off[mm] = off;
+            p.sub_piece_slot[mm] = tile_swz(local);
+        }
     }
     return p;
 }
