@@ -38,10 +38,11 @@ double batch_cost(const Partition& part, const std::vector<hq_gate>& gates, int 
 }  // namespace
 
 // Tiles per work item: about four items per resident block and level, at most
-// 64 tiles (4 MiB of amplitudes) per item.
+// 16 tiles (1 MiB of amplitudes) per item, so that the blocks finish a launch
+// within about one item of each other.
 uint32_t batch_chunk_tiles(uint64_t tiles, int slots) {
     const uint64_t c = tiles / (4 * uint64_t(std::max(1, slots)));
-    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 1), 64);
+    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 1), 16);
 }
 
 void batch_release(hq_batch_s* b) {

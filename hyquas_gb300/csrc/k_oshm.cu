@@ -40,16 +40,6 @@ __host__ __device__ __forceinline__ uint32_t swz(uint32_t x) { return tile_swz(x
 // .f32x2, sm_100+): a v2 holds two fp32 values and never round-trips
 // through a float pair.
 typedef unsigned long long v2;
-__device__ __forceinline__ v2 vadd(v2 a, v2 b) {
-    v2 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ v2 vsub(v2 a, v2 b) {
-    v2 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
 __device__ __forceinline__ v2 vmul(v2 a, v2 b) {
     v2 d;
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
@@ -127,9 +117,6 @@ __device__ __forceinline__ void ip_cmul(v2& r, v2& i, v2 er, v2 ei, v2 ein) {
         "mul.rn.f32x2 %1, %2, %1;\n\tfma.rn.f32x2 %1, %3, %0, %1;\n\t"
         "mov.b64 %0, t;\n\t}"
         : "+l"(r), "+l"(i) : "l"(er), "l"(ei), "l"(ein));
-}
-__device__ __forceinline__ void ip_scale(v2& x, v2 f) {
-    asm("mul.rn.f32x2 %0, %1, %0;" : "+l"(x) : "l"(f));
 }
 __device__ __forceinline__ void ip_xor(v2& x, v2 m) { asm("xor.b64 %0, %0, %1;" : "+l"(x) : "l"(m)); }
 // general complex 2x2: l' = a l + b h, h' = c l + d h (x = re, y = im, n = -im)
