@@ -162,3 +162,18 @@ def test_batch_bounded_wait_reports_timeout(hq, oracle):
     b.run(zero_init=True)
     for (n, desc), s in zip(circuits, states):
         check(oracle, oracle.run_f64(n, desc), s.store())
+
+
+def test_batch_empty_and_single_tile(hq, oracle):
+    """An empty batch runs as a no-op; a lone 10-qubit circuit is one tile and
+    one group (every qubit local)."""
+    b = hq.Batch()
+    b.compile()
+    assert b.info()["circuits"] == 0 and b.info()["items"] == 0
+    b.run()
+    circuits = [(10, W.ry_rz_cz(W.SplitMix64(101), 10, 12))]
+    b2, states, _ = make_batch(hq, circuits)
+    info = b2.info()
+    assert info["groups"] == 1 and info["items"] == 1 and info["tile_qubits"] == [10]
+    b2.run()
+    check(oracle, oracle.run_f64(*circuits[0]), states[0].store())

@@ -299,3 +299,42 @@ def test_qft28_analytic_amplitudes(hq, oracle):
     N = float(1 << n)
     ref = np.exp(2j * np.pi * ((x * ks.astype(np.float64)) % N) / N) / math.sqrt(N)
     assert np.max(np.abs(got - ref)) < 1e-6
+
+
+def test_max_size_34_qubits(hq, oracle):
+    """The largest register on one GB300 (2^34 amplitudes, 128 GiB): 64-bit
+    indexing through the OShareMem path, the readout, the FP64 reductions and
+    the sampler.  H on every qubit, RZ on every qubit and CZ on a matching give
+    amp(x) = 2^(-n/2) prod_q exp(-+i theta_q/2) prod_(a,b) (-1)^(x_a x_b);
+    the inverse circuit then returns |0...0>."""
+    n = 34
+    rng = W.SplitMix64(34)
+    theta = [rng.uniform() * W.TWO_PI for _ in range(n)]
+    pairs = [(2 * i, 2 * i + 1) for i in range(n // 2)]
+    desc = [(W.H, q, -1, -1, ()) for q in range(n)]
+    desc += [(W.RZ, q, -1, -1, (theta[q],)) for q in range(n)]
+    desc += [(W.CZ, b, a, -1, ()) for a, b in pairs]
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile(backend="oshm")
+    s = hq.State(n)
+    c.run_on(s)
+    xs = np.array([0, 1, (1 << n) - 1, 0x2_5A5A_5A5A] + [int(v) << 11 | 0x3FF for v in
+                   W.SplitMix64(7).shuffle(range(1 << 20))[:60]], dtype=np.uint64)
+    got = s.amps(xs)
+    for x, a in zip(xs.tolist(), got):
+        ph = sum((theta[q] / 2) * (1 if (x >> q) & 1 else -1) for q in range(n))
+        sign = (-1) ** sum(((x >> p) & 1) & ((x >> q) & 1) for p, q in pairs)
+        ref = sign * np.exp(1j * ph) / math.sqrt(2.0 ** n)
+        assert abs(a - ref) < 1e-9 + 1e-5 * abs(ref)
+    assert abs(s.norm() - 1.0) < 1e-4
+    assert np.max(np.abs(s.marginals() - 0.5)) < 1e-4
+    shots = s.sample(64, seed=3)
+    assert shots.size == 64 and int(shots.max()) < (1 << n)
+    ci = hq.Circuit(n)
+    ci.addGates(W.to_gates(inverse(desc)))
+    ci.compile(backend="oshm")
+    ci.run_on(s)
+    amp0 = s.amps(np.array([0], dtype=np.uint64))[0]
+    assert abs(abs(amp0) ** 2 - 1.0) < 1e-4
+    s.free()
