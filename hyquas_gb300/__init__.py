@@ -57,6 +57,11 @@ class hq_compile_options(C.Structure):
                 ("reference_grouping", C.c_int32), ("specialize", C.c_int32)]
 
 
+class hq_cost_params(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("pass_floor", "oshm_gate", "oshm_diag", "oshm_ctrl_diag",
+                                         "mm_bf16x3", "mm_tf32", "mm_fp32", "launch")]
+
+
 class hq_server_options(C.Structure):
     _fields_ = [("hbm_budget", C.c_uint64), ("step_budget_us", C.c_double),
                 ("planner_threads", C.c_int32), ("tile_qubits", C.c_int32)]
@@ -111,6 +116,9 @@ def _load():
         "hq_apply_unitary": [P, P, U64, I32],
         "hq_group_unitary": [P, I32, U64, P],
         "hq_qasm_parse": [C.c_char_p, C.POINTER(I32), P, I32, C.POINTER(I32)],
+        "hq_cost_params_get": [C.POINTER(hq_cost_params)],
+        "hq_cost_params_set": [C.POINTER(hq_cost_params)],
+        "hq_autotune": [I32, C.POINTER(hq_cost_params)],
         "hq_server_options_default": [C.POINTER(hq_server_options)],
         "hq_server_check": [C.POINTER(hq_server_options), I32, P, I32],
         "hq_server_create": [C.POINTER(hq_server_options), C.POINTER(P)],
@@ -296,6 +304,29 @@ def gate_array(gates) -> C.Array:
     for i, g in enumerate(gates):
         arr[i] = g.g if isinstance(g, Gate) else g
     return arr
+
+
+def cost_params() -> dict:
+    """The cost model's constants (seconds per amplitude per pass, and per launch)."""
+    p = hq_cost_params()
+    check(lib.hq_cost_params_get(C.byref(p)))
+    return {k: getattr(p, k) for k, _ in hq_cost_params._fields_}
+
+
+def set_cost_params(params: dict):
+    p = hq_cost_params()
+    check(lib.hq_cost_params_get(C.byref(p)))
+    for k, v in params.items():
+        setattr(p, k, float(v))
+    check(lib.hq_cost_params_set(C.byref(p)))
+
+
+def autotune(num_qubits: int = 0) -> dict:
+    """Measure the cost model on this GPU and install it (replaces the
+    reference's offline calibration and parameter files)."""
+    p = hq_cost_params()
+    check(lib.hq_autotune(num_qubits, C.byref(p)))
+    return {k: getattr(p, k) for k, _ in hq_cost_params._fields_}
 
 
 def parse_qasm(text: str) -> tuple[int, list]:
@@ -726,5 +757,6 @@ class Batch:
             pass
 
 
-__all__ = ["Circuit", "Batch", "Server", "Gate", "State", "parse_qasm", "ResultItem", "HQError", "init", "device_info",
+__all__ = ["Circuit", "Batch", "Server", "Gate", "State", "parse_qasm", "autotune",
+           "cost_params", "set_cost_params", "ResultItem", "HQError", "init", "device_info",
            "group_unitary", "set_hbm_budget", "hbm_in_use", "lib", "LIB_PATH"]

@@ -450,6 +450,29 @@ hq_status hq_qasm_parse(const char* text, int32_t* num_qubits, hq_gate* out, int
     HQ_API_END
 }
 
+// ---- cost model ---------------------------------------------------------------------
+
+hq_status hq_cost_params_get(hq_cost_params* out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(out);
+    *out = cost_params();
+    HQ_API_END
+}
+
+hq_status hq_cost_params_set(const hq_cost_params* p) {
+    HQ_API_BEGIN
+    HQ_NONNULL(p);
+    set_cost_params(*p);
+    HQ_API_END
+}
+
+hq_status hq_autotune(int32_t num_qubits, hq_cost_params* out) {
+    HQ_API_BEGIN
+    const hq_cost_params p = autotune(num_qubits);
+    if (out) *out = p;
+    HQ_API_END
+}
+
 // ---- batches ------------------------------------------------------------------------
 
 hq_status hq_batch_create(hq_batch* out) {

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <mutex>
 #include <cstring>
 
 namespace hq {
@@ -692,39 +693,54 @@ OshmLaunch make_oshm_launch(const OshmProgram& prog, void* state, const OshmPhas
 }
 
 // ---- GB300 cost model --------------------------------------------------------
-// Seconds per pass over 2^n amplitudes, fitted to CUDA-event times of the
-// kernels on a GB300 (30-qubit grid circuit, 28-qubit QFT; see the design
-// notes): a pass costs its HBM floor (16 B per amplitude at the measured copy
-// bandwidth) plus, for OShareMem, FP32 work per gate.  Replaces the
-// reference's V100 tables (src/evaluator.h:18-127, src/evaluator.cpp:111-229).
-static const double kPassFloor = 2.4e-12;       // s per amplitude: 16 B at 6.7 TB/s
-static const double kOshmGate = 6.6e-14;        // s per amplitude per non-diagonal gate
-static const double kOshmDiag = 0.3 * 6.6e-14;  // uncontrolled diagonal gate
-static const double kOshmCtrlDiag = 1.4 * 6.6e-14;  // controlled diagonal gate
-static const double kMmBf16x3 = 5.4e-12;        // s per amplitude per 6-qubit TransMM pass
-static const double kMmTf32 = 4.6e-12;
-static const double kMmFp32 = 1.5e-11;
-static const double kLaunchSec = 4e-6;
+// Seconds per pass over 2^n amplitudes: a pass costs its HBM floor (16 B per
+// amplitude at the copy bandwidth) plus, for OShareMem, FP32 work per gate.
+// The defaults are fitted to CUDA-event times of the kernels on a GB300
+// (30-qubit grid circuit, 28-qubit QFT); hq_autotune measures them on the GPU
+// at hand (autotune.cpp).  Replaces the reference's V100 tables and their
+// calibrator (src/evaluator.h:18-127, src/evaluator.cpp:111-229,
+// evaluator-preprocess/process.cpp:24-176).
+namespace {
+std::mutex g_cost_mu;
+hq_cost_params g_cost = {2.4e-12, 6.6e-14, 0.3 * 6.6e-14, 1.4 * 6.6e-14,
+                         5.4e-12, 4.6e-12, 1.5e-11,       4e-6};
+}  // namespace
+
+hq_cost_params cost_params() {
+    std::lock_guard<std::mutex> lk(g_cost_mu);
+    return g_cost;
+}
+
+void set_cost_params(const hq_cost_params& p) {
+    const double v[] = {p.pass_floor, p.oshm_gate, p.oshm_diag, p.oshm_ctrl_diag,
+                        p.mm_bf16x3,  p.mm_tf32,   p.mm_fp32,   p.launch};
+    for (double x : v)
+        HQ_REQUIRE(std::isfinite(x) && x >= 0.0 && x < 1.0, HQ_ERR_INVALID, "cost parameter %g out of range", x);
+    std::lock_guard<std::mutex> lk(g_cost_mu);
+    g_cost = p;
+}
 
 double cost_oshm(int n, int nphases, const std::vector<hq_gate>& gates, int k) {
     (void)k;
     (void)nphases;
+    const hq_cost_params c = cost_params();
     const double amps = double(uint64_t(1) << n);
     double w = 0;
     for (const auto& g : gates) {
         if (!matrix_is_diagonal(g))
-            w += kOshmGate;
+            w += c.oshm_gate;
         else
-            w += g.control >= 0 ? kOshmCtrlDiag : kOshmDiag;
+            w += g.control >= 0 ? c.oshm_ctrl_diag : c.oshm_diag;
     }
-    return amps * (kPassFloor + w) + kLaunchSec;
+    return amps * (c.pass_floor + w) + c.launch;
 }
 
 double cost_transmm(int n, int m, int precision) {
+    const hq_cost_params c = cost_params();
     const double amps = double(uint64_t(1) << n);
-    double per = precision == HQ_MM_FP32 ? kMmFp32 : (precision == HQ_MM_TF32 ? kMmTf32 : kMmBf16x3);
+    double per = precision == HQ_MM_FP32 ? c.mm_fp32 : (precision == HQ_MM_TF32 ? c.mm_tf32 : c.mm_bf16x3);
     if (precision == HQ_MM_FP32 && m > 6) per *= double(1 << (m - 6));  // SIMT flops grow with 2^m
-    return amps * per + kLaunchSec;
+    return amps * per + c.launch;
 }
 
 }  // namespace hq

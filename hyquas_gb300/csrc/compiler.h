@@ -46,6 +46,9 @@ Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<
 
 // GB300 cost model (seconds) used by the hybrid backend; the constants are
 // fitted to kernel timings on GB300 (compiler.cpp).
+hq_cost_params cost_params();
+void set_cost_params(const hq_cost_params& p);
+hq_cost_params autotune(int n);  // autotune.cpp: measure and install the parameters
 double cost_oshm(int n, int nphases, const std::vector<hq_gate>& gates, int k);
 double cost_transmm(int n, int m, int precision);
 

@@ -239,6 +239,28 @@ hq_status hq_circuit_enqueue(hq_circuit c, hq_state s);
 hq_status hq_circuit_capture_graph(hq_circuit c, hq_state s);
 hq_status hq_synchronize(void);
 
+/* ---- cost model and autotuner (replace the reference's V100/A100 parameter
+ * files and their calibrator: src/evaluator.h:18-127, src/evaluator.cpp:111-229,
+ * evaluator-preprocess/process.cpp:24-176) ---------------------------------
+ * Seconds per amplitude of one pass over the state; the hybrid partitioner
+ * and the batch/serving planners predict group times with them. */
+typedef struct hq_cost_params {
+    double pass_floor;      /* OShareMem pass without gates (HBM read + write) */
+    double oshm_gate;       /* + per non-diagonal gate */
+    double oshm_diag;       /* + per uncontrolled diagonal gate */
+    double oshm_ctrl_diag;  /* + per controlled diagonal gate */
+    double mm_bf16x3;       /* 6-qubit TransMM pass, split BF16 (tensor cores) */
+    double mm_tf32;         /* 6-qubit TransMM pass, TF32 (tensor cores) */
+    double mm_fp32;         /* 6-qubit TransMM pass, FP32 SIMT (x 2^(m-6) beyond 6) */
+    double launch;          /* seconds per launch */
+} hq_cost_params;
+hq_status hq_cost_params_get(hq_cost_params* out);
+hq_status hq_cost_params_set(const hq_cost_params* p);
+/* Measure the parameters on this GPU with a num_qubits-qubit scratch state
+ * (0 = 26; a few seconds, including kernel generation) and install them;
+ * *out (may be NULL) receives them, e.g. to save and set again later. */
+hq_status hq_autotune(int32_t num_qubits, hq_cost_params* out);
+
 /* ---- batched execution (no reference counterpart: the reference runs one
  * circuit per process, src/circuit.cpp:16-71) ------------------------------
  * Many circuits of uneven qubit counts run in ONE persistent launch that pulls

@@ -1,0 +1,53 @@
+"""The cost model's parameters (host) and the autotuner that measures them
+(GPU).  They replace the reference's per-GPU parameter files and their
+calibrator (src/evaluator.cpp:98-107, evaluator-preprocess/process.cpp)."""
+import pytest
+
+import hyquas_gb300 as hq
+from hyquas_gb300 import workloads as W
+
+
+def test_params_round_trip_and_validation():
+    p0 = hq.cost_params()
+    assert all(v > 0 for v in p0.values())
+    try:
+        hq.set_cost_params({"oshm_gate": 1e-13})
+        assert hq.cost_params()["oshm_gate"] == 1e-13
+        with pytest.raises(hq.HQError):
+            hq.set_cost_params({"pass_floor": -1.0})
+        assert hq.cost_params()["pass_floor"] == p0["pass_floor"]  # rejected: unchanged
+    finally:
+        hq.set_cost_params(p0)
+
+
+def test_params_drive_the_hybrid_choice():
+    """A cheap TransMM makes the hybrid partitioner pick it; an expensive one
+    makes it pick OShareMem (host-only planning)."""
+    import ctypes as C
+    from test_partition import plan
+    p0 = hq.cost_params()
+    desc = W.qft(16)
+    try:
+        hq.set_cost_params({"mm_bf16x3": 1e-15, "mm_tf32": 1e-15, "mm_fp32": 1e-15, "launch": 0.0})
+        g1 = plan(16, desc, hq.BACKEND_HYBRID, reference=False)
+        hq.set_cost_params({"mm_bf16x3": 1e-6, "mm_tf32": 1e-6, "mm_fp32": 1e-6})
+        g2 = plan(16, desc, hq.BACKEND_HYBRID, reference=False)
+    finally:
+        hq.set_cost_params(p0)
+    assert any(g["backend"] == hq.BACKEND_TRANSMM for g in g1)
+    assert all(g["backend"] == hq.BACKEND_OSHM for g in g2)
+
+
+@pytest.mark.gpu
+def test_autotune_measures_plausible_constants(hq):
+    p0 = hq.cost_params()
+    try:
+        p = hq.autotune(24)
+        assert p == hq.cost_params()  # installed
+        # HBM floor: 16 B per amplitude at 1..10 TB/s
+        assert 1.6e-12 < p["pass_floor"] < 1.6e-11, p
+        assert 0 <= p["oshm_diag"] < p["oshm_gate"] < 1e-11, p
+        assert 0 < p["mm_tf32"] and 0 < p["mm_bf16x3"] < p["mm_fp32"], p
+        assert 0 < p["launch"] < 1e-3, p
+    finally:
+        hq.set_cost_params(p0)
