@@ -130,6 +130,7 @@ def _load():
         "hq_server_times": [P, I64, C.POINTER(D), C.POINTER(D), C.POINTER(D)],
         "hq_server_release": [P, I64],
         "hq_server_steps": [P, I64, C.POINTER(I64), C.POINTER(I64)],
+        "hq_server_plan_cache": [P, C.POINTER(I64), C.POINTER(I64)],
         "hq_server_stats": [P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64), C.POINTER(U64),
                             C.POINTER(U64)],
         "hq_batch_create": [C.POINTER(P)],
@@ -679,6 +680,11 @@ class Server:
         check(lib.hq_server_stats(self._h, *[C.byref(x) for x in v]))
         return dict(zip(["steps", "items", "finished", "resident_bytes", "peak_resident_bytes"],
                         [x.value for x in v]))
+
+    def plan_cache(self) -> dict:
+        h, e = C.c_int64(), C.c_int64()
+        check(lib.hq_server_plan_cache(self._h, C.byref(h), C.byref(e)))
+        return {"hits": h.value, "entries": e.value}
 
     def close(self):
         if self._h:

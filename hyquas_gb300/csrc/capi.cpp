@@ -666,6 +666,15 @@ hq_status hq_server_steps(hq_server sv, int64_t id, int64_t* first_step, int64_t
     HQ_API_END
 }
 
+hq_status hq_server_plan_cache(hq_server sv, int64_t* hits, int64_t* entries) {
+    HQ_API_BEGIN
+    HQ_NONNULL(sv);
+    std::lock_guard<std::mutex> lk(sv->cache_mu);
+    if (hits) *hits = sv->cache_hits;
+    if (entries) *entries = (int64_t)sv->plan_cache.size();
+    HQ_API_END
+}
+
 hq_status hq_server_release(hq_server sv, int64_t id) {
     HQ_API_BEGIN
     HQ_NONNULL(sv);

@@ -45,6 +45,25 @@ void check_request(const hq_server_options& o, int n, const hq_gate* gates, int 
                (unsigned long long)bytes, (unsigned long long)o.hbm_budget);
 }
 
+// Plans are cached by circuit (qubit count, gate records, tile option): a
+// request whose circuit was planned before reuses that plan.
+uint64_t plan_key(const Request* r, int fixed_k) {
+    uint64_t h = 1469598103934665603ull;  // FNV-1a
+    auto mix = [&](const void* p, size_t n) {
+        const unsigned char* b = (const unsigned char*)p;
+        for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 1099511628211ull;
+    };
+    mix(&r->n, sizeof(r->n));
+    mix(&fixed_k, sizeof(fixed_k));
+    if (!r->gates.empty()) mix(r->gates.data(), sizeof(hq_gate) * r->gates.size());
+    return h;
+}
+
+bool same_gates(const std::vector<hq_gate>& a, const std::vector<hq_gate>& b) {
+    return a.size() == b.size() &&
+           (a.empty() || std::memcmp(a.data(), b.data(), sizeof(hq_gate) * a.size()) == 0);
+}
+
 void plan_request(Request* r, int fixed_k) {
     std::vector<int> perm;
     std::vector<hq_gate> folded = fold_swaps(r->gates, r->n, perm);
@@ -79,7 +98,41 @@ void planner_main(hq_server_s* sv) {
         }
         std::string err;
         try {
-            plan_request(r, sv->opt.tile_qubits);
+            const uint64_t key = plan_key(r, sv->opt.tile_qubits);
+            std::shared_ptr<const PlanEntry> hit;
+            {
+                std::lock_guard<std::mutex> lk(sv->cache_mu);
+                auto it = sv->plan_cache.find(key);
+                if (it != sv->plan_cache.end() && it->second->n == r->n &&
+                    same_gates(it->second->gates, r->gates))
+                    hit = it->second;
+            }
+            if (hit) {
+                r->progs = hit->progs;
+                r->group_cost = hit->group_cost;
+                r->swap_perm = hit->swap_perm;
+                r->k = hit->k;
+                std::lock_guard<std::mutex> lk(sv->cache_mu);
+                sv->cache_hits++;
+            } else {
+                plan_request(r, sv->opt.tile_qubits);
+                auto e = std::make_shared<PlanEntry>();
+                e->n = r->n;
+                e->gates = r->gates;
+                e->progs = r->progs;
+                e->group_cost = r->group_cost;
+                e->swap_perm = r->swap_perm;
+                e->k = r->k;
+                std::lock_guard<std::mutex> lk(sv->cache_mu);
+                if (!sv->plan_cache.count(key)) {
+                    sv->plan_cache[key] = e;
+                    sv->cache_order.push_back(key);
+                    while (sv->cache_order.size() > kPlanCacheEntries) {
+                        sv->plan_cache.erase(sv->cache_order.front());
+                        sv->cache_order.pop_front();
+                    }
+                }
+            }
         } catch (const std::exception& e) {
             err = e.what();
         }

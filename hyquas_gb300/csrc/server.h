@@ -46,6 +46,17 @@ struct Request {
     uint64_t state_bytes = 0, resident_bytes = 0;
 };
 
+// A cached plan: the circuit it is for and its lowered groups.
+struct PlanEntry {
+    int n = 0;
+    std::vector<hq_gate> gates;
+    std::vector<OshmProgram> progs;
+    std::vector<double> group_cost;
+    std::vector<int> swap_perm;
+    int k = 0;
+};
+constexpr size_t kPlanCacheEntries = 256;
+
 // One step's staging: pinned host copy of launches, items and new programs,
 // their device copy, and the completion event.
 struct StepBuf {
@@ -80,6 +91,10 @@ struct hq_server_s {
     int* d_err = nullptr;
     int slots = 0;
     hq::StepBuf buf[2];
+    std::mutex cache_mu;  // plan cache (planner threads)
+    std::unordered_map<uint64_t, std::shared_ptr<const hq::PlanEntry>> plan_cache;
+    std::deque<uint64_t> cache_order;
+    int64_t cache_hits = 0;
     std::chrono::steady_clock::time_point t0;
 };
 

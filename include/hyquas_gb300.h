@@ -341,6 +341,9 @@ hq_status hq_server_times(hq_server sv, int64_t id, double* submit_us, double* a
 /* Index of the first and last step (batched launch) the request ran in; two
  * requests whose ranges meet shared a launch. */
 hq_status hq_server_steps(hq_server sv, int64_t id, int64_t* first_step, int64_t* last_step);
+/* Plan cache: requests whose circuit (qubit count and gate records) was
+ * planned before reuse that plan.  Hits so far and cached plans. */
+hq_status hq_server_plan_cache(hq_server sv, int64_t* hits, int64_t* entries);
 /* Frees the request's state (finished requests only). */
 hq_status hq_server_release(hq_server sv, int64_t id);
 hq_status hq_server_stats(hq_server sv, int64_t* steps, int64_t* items, int64_t* finished,

@@ -142,3 +142,20 @@ def test_sampler_honours_layout(hq, oracle):
     got = s.sample(2000, seed=9)
     ref = oracle.sample(oracle.run_f64(n, desc).astype(np.complex64), 2000, 9)
     assert np.mean(got == ref) >= 0.99
+
+
+def test_plan_cache_reuses_plans(hq, oracle):
+    """A circuit submitted again is not planned again, and gives the same result."""
+    rng = W.SplitMix64(123)
+    desc = W.ry_rz_cz(rng, 16, 12)
+    arr = hq.gate_array(W.to_gates(desc))
+    sv = hq.Server()
+    first = sv.submit(16, arr)
+    a = drain(sv, [first])[first]
+    assert sv.plan_cache()["entries"] >= 1
+    second = sv.submit(16, arr)
+    b = drain(sv, [second])[second]
+    assert sv.plan_cache()["hits"] >= 1
+    assert np.array_equal(a, b)
+    check(oracle, oracle.run_f64(16, desc), b)
+    sv.close()
