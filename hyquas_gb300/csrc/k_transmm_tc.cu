@@ -107,6 +107,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&v)[8]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi) {
     return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
@@ -188,7 +197,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
     const uint64_t J = blockIdx.x < nsub ? (nsub - blockIdx.x + G - 1) / G : 0;
     auto sub_base = [&](uint64_t j) {
         const uint64_t v = blockIdx.x + j * G;
-        return tile_base(v >> 1, p.nruns, p.run_src, p.run_dst, p.run_len) + (v & 1) * p.split_off;
+        return tile_base(v >> 1, p.nruns, p.run_src, p.run_dst, p.run_len) + (v & 1) * p.split_off[0];
     };
     auto load = [&](uint64_t j) {
         if (j < J) {
@@ -334,6 +343,264 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));
 }
 
+// ---- 7-qubit groups ---------------------------------------------------------
+// U (128 x 128 complex) no longer fits shared memory in real form, so the
+// product is taken in complex form over four real GEMMs into two accumulators:
+//     Cr = Ur.Br + Ui.(-Bi),   Ci = Ui.Br + Ur.Bi      (M = 128, N = 16, K = 128)
+// A holds Ur and Ui (split BF16 hi + lo, or TF32; 128 KB); each sub-tile of
+// 128 rows x 16 columns stages Br, Bi and -Bi.  The pipeline is the one of the
+// 6-qubit kernel (three staging buffers, two B buffers, two accumulator pairs).
+constexpr int T7_ROWS = 128;
+constexpr int T7_NSUB = 16;
+constexpr uint32_t SUB7_BYTES = 16384;   // a sub-tile, float2[2048]
+constexpr uint32_t SM7_A = 0;            // Ur, Ui: 128 KB
+constexpr uint32_t SM7_UI = 65536;
+constexpr uint32_t SM7_B = 131072;       // two buffers of 24 KB: Br | Bi | -Bi
+constexpr uint32_t B7_BYTES = 24576;
+constexpr uint32_t SM7_R = 180224;       // three staging buffers of 16 KB
+constexpr uint32_t SM7_MISC = 229376;
+constexpr uint32_t SM7_TOTAL = SM7_MISC + 1024;
+constexpr uint32_t TMEM7_COLS = 64;      // two buffers x (Cr 16 + Ci 16 columns)
+static_assert(SM7_TOTAL <= 232448, "shared memory per block");
+
+template <int PREC>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc7(const TransmmLaunch p) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    uint32_t* rowslot = reinterpret_cast<uint32_t*>(smem + SM7_MISC + 64);
+    uint32_t* colslot = rowslot + T7_ROWS;
+    const uint32_t sb = smem_u32(smem);
+    const uint32_t s_mbar = sb + SM7_MISC;
+    const uint32_t s_tslot = sb + SM7_MISC + 16;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    float2* __restrict__ state = reinterpret_cast<float2*>(p.state);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_tslot),
+                     "r"(TMEM7_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar + 8));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    for (int r = t; r < T7_ROWS; r += TC_THREADS) {
+        uint32_t x = 0;
+        for (int b = 0; b < 7; b++)
+            if ((r >> b) & 1) x |= 1u << p.row_sub[b];
+        rowslot[r] = tile_swz(x);
+    }
+    for (int c = t; c < T7_NSUB; c += TC_THREADS) {
+        uint32_t x = 0;
+        for (int b = 0; b < 4; b++)
+            if ((c >> b) & 1) x |= 1u << p.col_sub[b];
+        colslot[c] = tile_swz(x);
+    }
+    const char* asrc = reinterpret_cast<const char*>(p.umat);
+    for (int i = t; i < 8192; i += TC_THREADS) cp_async16(sb + SM7_A + i * 16u, asrc + i * 16);
+    cp_async_commit();
+    cp_async_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + SM7_MISC + 16);
+
+    const uint64_t toff = local_to_phys(uint32_t(t) << 1, TC_TILE_BITS - 2, p.sub_phys);
+    const uint32_t tsl = tile_swz(uint32_t(t) << 1);
+    constexpr uint32_t esize = PREC == HQ_MM_TF32 ? 4 : 2;
+    constexpr uint32_t kstep_bytes = 256;
+    constexpr uint32_t sbo = (128 / (16 / esize)) * 128;
+    constexpr uint32_t a_lo = 32768;          // Ur / Ui lo halves (BF16x3)
+    constexpr uint32_t b_lo = 4096;           // Br / Bi / -Bi lo halves (BF16x3)
+    constexpr uint32_t idesc = make_idesc(PREC == HQ_MM_TF32 ? 2u : 1u, 128, T7_NSUB);
+    constexpr int nsteps = PREC == HQ_MM_TF32 ? 16 : 8;
+
+    const uint64_t nsub = p.ntiles * 4;
+    const uint64_t G = gridDim.x;
+    const uint64_t J = blockIdx.x < nsub ? (nsub - blockIdx.x + G - 1) / G : 0;
+    auto sub_base = [&](uint64_t j) {
+        const uint64_t v = blockIdx.x + j * G;
+        return tile_base(v >> 2, p.nruns, p.run_src, p.run_dst, p.run_len) +
+               (v & 1) * p.split_off[0] + ((v >> 1) & 1) * p.split_off[1];
+    };
+    auto load = [&](uint64_t j) {
+        if (j < J) {
+            const float2* gsrc = state + sub_base(j) + toff;
+            const uint32_t rb = sb + SM7_R + uint32_t(j % 3) * SUB7_BYTES;
+#pragma unroll
+            for (int m = 0; m < 4; m++)
+                cp_async16(rb + (tsl ^ p.sub_piece_slot[m]) * 8u, gsrc + p.sub_piece_off[m]);
+        }
+        cp_async_commit();
+    };
+    bool failed = false;
+    // results of sub-tile j: (Cr, Ci) in TMEM columns 32 (j&1) and + 16 -> staging -> HBM
+    auto epilogue = [&](uint64_t j) {
+        const uint32_t b = uint32_t(j & 1);
+        const bool ok = mbar_wait(s_mbar + 8 * b, uint32_t((j >> 1) & 1));
+        if (__syncthreads_or(!ok)) {
+            if (t == 0 && p.err) {
+                atomicCAS(p.err, 0, 1);
+                p.err[1] = 7;  // site: TransMM accumulator wait
+                p.err[2] = (int)(j & 0x7fffffff);
+            }
+            failed = true;
+            return;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        float2* Rj = reinterpret_cast<float2*>(smem + SM7_R + uint32_t(j % 3) * SUB7_BYTES);
+        {
+            const int q = warp & 3, half = warp >> 2;
+            const int i = 32 * q + lane;  // D row = TMEM lane = row of the group
+            const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + 32 * b + 8 * half;
+            uint32_t vr[8], vi[8];
+            tmem_ld8(col, vr);
+            tmem_ld8(col + 16, vi);
+            const uint32_t rs = rowslot[i];
+#pragma unroll
+            for (int c = 0; c < 8; c++)
+                Rj[rs ^ colslot[8 * half + c]] = make_float2(__uint_as_float(vr[c]), __uint_as_float(vi[c]));
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        float2* gdst = state + sub_base(j) + toff;
+        const float4* R4 = reinterpret_cast<const float4*>(Rj);
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+            *reinterpret_cast<float4*>(gdst + p.sub_piece_off[m]) = R4[(tsl ^ p.sub_piece_slot[m]) >> 1];
+        __syncthreads();
+    };
+
+    load(0);
+    load(1);
+    for (uint64_t j = 0; j < J && !failed; j++) {
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncthreads();
+        // B blocks of sub-tile j: row n of each = column n; K = the group's row
+        {
+            const float2* Rj = reinterpret_cast<const float2*>(smem + SM7_R + uint32_t(j % 3) * SUB7_BYTES);
+            unsigned char* B = smem + SM7_B + uint32_t(j & 1) * B7_BYTES;
+            const int n = t & 15, rb = t >> 4;
+            const uint32_t cs = colslot[n];
+            float re[8], im[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const float2 a = Rj[rowslot[rb * 8 + q] ^ cs];
+                re[q] = a.x;
+                im[q] = a.y;
+            }
+            if (PREC == HQ_MM_TF32) {
+#pragma unroll
+                for (int half = 0; half < 2; half++) {
+                    const uint32_t o = kmajor_off(n, rb * 8 + half * 4, 128, 4);
+                    const float4 vr = make_float4(to_tf32(re[4 * half]), to_tf32(re[4 * half + 1]),
+                                                  to_tf32(re[4 * half + 2]), to_tf32(re[4 * half + 3]));
+                    const float4 vi = make_float4(to_tf32(im[4 * half]), to_tf32(im[4 * half + 1]),
+                                                  to_tf32(im[4 * half + 2]), to_tf32(im[4 * half + 3]));
+                    *reinterpret_cast<float4*>(B + o) = vr;
+                    *reinterpret_cast<float4*>(B + 8192 + o) = vi;
+                    *reinterpret_cast<float4*>(B + 16384 + o) = make_float4(-vi.x, -vi.y, -vi.z, -vi.w);
+                }
+            } else {
+                uint32_t hre[4], lre[4], him[4], lim[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const __nv_bfloat16 h0 = __float2bfloat16_rn(re[2 * q]);
+                    const __nv_bfloat16 h1 = __float2bfloat16_rn(re[2 * q + 1]);
+                    const __nv_bfloat16 l0 = __float2bfloat16_rn(re[2 * q] - __bfloat162float(h0));
+                    const __nv_bfloat16 l1 = __float2bfloat16_rn(re[2 * q + 1] - __bfloat162float(h1));
+                    hre[q] = pack_bf16(h0, h1);
+                    lre[q] = pack_bf16(l0, l1);
+                    const __nv_bfloat16 g0 = __float2bfloat16_rn(im[2 * q]);
+                    const __nv_bfloat16 g1 = __float2bfloat16_rn(im[2 * q + 1]);
+                    const __nv_bfloat16 k0 = __float2bfloat16_rn(im[2 * q] - __bfloat162float(g0));
+                    const __nv_bfloat16 k1 = __float2bfloat16_rn(im[2 * q + 1] - __bfloat162float(g1));
+                    him[q] = pack_bf16(g0, g1);
+                    lim[q] = pack_bf16(k0, k1);
+                }
+                const uint32_t o = kmajor_off(n, rb * 8, 128, 2);
+                const uint32_t sg = 0x80008000u;  // BF16 sign bits: -Bi exactly
+                *reinterpret_cast<uint4*>(B + o) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+                *reinterpret_cast<uint4*>(B + b_lo + o) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
+                *reinterpret_cast<uint4*>(B + 8192 + o) = make_uint4(him[0], him[1], him[2], him[3]);
+                *reinterpret_cast<uint4*>(B + 8192 + b_lo + o) = make_uint4(lim[0], lim[1], lim[2], lim[3]);
+                *reinterpret_cast<uint4*>(B + 16384 + o) =
+                    make_uint4(him[0] ^ sg, him[1] ^ sg, him[2] ^ sg, him[3] ^ sg);
+                *reinterpret_cast<uint4*>(B + 16384 + b_lo + o) =
+                    make_uint4(lim[0] ^ sg, lim[1] ^ sg, lim[2] ^ sg, lim[3] ^ sg);
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+
+        if (t == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t dr = tmem + 32 * uint32_t(j & 1), di = dr + 16;
+            const uint32_t bb = sb + SM7_B + uint32_t(j & 1) * B7_BYTES;
+            const uint32_t ur = sb + SM7_A, ui = sb + SM7_UI;
+            const uint32_t br = bb, bi = bb + 8192, bn = bb + 16384;
+            // D += A . B over K = 128; first = the accumulator starts at zero
+            auto gemm = [&](uint32_t d, uint32_t a, uint32_t bm, bool first) {
+                if (PREC == HQ_MM_TF32) {
+                    for (int kk = 0; kk < nsteps; kk++)
+                        mma_tf32(d, make_desc(a + kk * kstep_bytes, 128, sbo),
+                                 make_desc(bm + kk * kstep_bytes, 128, sbo), idesc, !first || kk > 0);
+                } else {
+                    for (int kk = 0; kk < nsteps; kk++)  // hi . hi
+                        mma_f16(d, make_desc(a + kk * kstep_bytes, 128, sbo),
+                                make_desc(bm + kk * kstep_bytes, 128, sbo), idesc, !first || kk > 0);
+                    for (int kk = 0; kk < nsteps; kk++)  // hi . lo
+                        mma_f16(d, make_desc(a + kk * kstep_bytes, 128, sbo),
+                                make_desc(bm + b_lo + kk * kstep_bytes, 128, sbo), idesc, 1);
+                    for (int kk = 0; kk < nsteps; kk++)  // lo . hi
+                        mma_f16(d, make_desc(a + a_lo + kk * kstep_bytes, 128, sbo),
+                                make_desc(bm + kk * kstep_bytes, 128, sbo), idesc, 1);
+                }
+            };
+            gemm(dr, ur, br, true);
+            gemm(dr, ui, bn, false);
+            gemm(di, ui, br, true);
+            gemm(di, ur, bi, false);
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                    s_mbar + 8 * uint32_t(j & 1))
+                : "memory");
+        }
+        if (j > 0) epilogue(j - 1);
+        if (failed) break;
+        load(j + 2);
+    }
+    if (!failed && J > 0) epilogue(J - 1);
+    cp_async_wait_all();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM7_COLS));
+}
+
+// A operand of a 7-qubit group from U (128 x 128, column-major complex128):
+// Ur and Ui, each 128 x 128 K-major (split BF16 hi at +0 and lo at +32 KB
+// of its 64 KB half, or TF32).
+__global__ void k_u_to_tc7(const double2* __restrict__ U, unsigned char* __restrict__ out, int prec) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 128 * 128) return;
+    const int r = idx / 128, k = idx % 128;
+    const double2 u = U[(size_t)k * 128 + r];
+    const double v[2] = {u.x, u.y};
+    for (int part = 0; part < 2; part++) {
+        unsigned char* base = out + part * 65536;
+        if (prec == HQ_MM_TF32) {
+            *reinterpret_cast<float*>(base + kmajor_off(r, k, 128, 4)) = to_tf32((float)v[part]);
+        } else {
+            const __nv_bfloat16 hi = __float2bfloat16_rn((float)v[part]);
+            const __nv_bfloat16 lo = __float2bfloat16_rn((float)(v[part] - (double)__bfloat162float(hi)));
+            *reinterpret_cast<__nv_bfloat16*>(base + kmajor_off(r, k, 128, 2)) = hi;
+            *reinterpret_cast<__nv_bfloat16*>(base + 32768 + kmajor_off(r, k, 128, 2)) = lo;
+        }
+    }
+}
+
 // A operand from the FP64 unitary U (64 x 64, column-major): the real form
 // [[Ur, -Ui], [Ui, Ur]] (128 x 128) in the K-major core layout.
 __global__ void k_u_to_tc(const double2* __restrict__ U, unsigned char* __restrict__ out, int prec) {
@@ -361,13 +628,18 @@ __global__ void k_u_to_tc(const double2* __restrict__ U, unsigned char* __restri
 
 size_t transmm_tc_operand_bytes(int m, int precision) {
     (void)precision;
-    HQ_REQUIRE(m == 6, HQ_ERR_UNSUPPORTED, "tensor-core TransMM runs 6-qubit groups (got %d)", m);
-    return 65536;
+    HQ_REQUIRE(m == 6 || m == 7, HQ_ERR_UNSUPPORTED,
+               "tensor-core TransMM runs 6- and 7-qubit groups (got %d)", m);
+    return m == 6 ? 65536 : 131072;
 }
 
 void launch_u_to_tc_operand(int m, int precision, const double* d_u, void* d_out, cudaStream_t st) {
-    HQ_REQUIRE(m == 6, HQ_ERR_UNSUPPORTED, "tensor-core TransMM runs 6-qubit groups (got %d)", m);
-    k_u_to_tc<<<64, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
+    HQ_REQUIRE(m == 6 || m == 7, HQ_ERR_UNSUPPORTED,
+               "tensor-core TransMM runs 6- and 7-qubit groups (got %d)", m);
+    if (m == 6)
+        k_u_to_tc<<<64, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
+    else
+        k_u_to_tc7<<<64, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -385,13 +657,33 @@ static void launch_prec(const TransmmLaunch& p, cudaStream_t st) {
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 
+template <int PREC>
+static void launch_prec7(const TransmmLaunch& p, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        HQ_CHECK_CUDA(cudaFuncSetAttribute(k_transmm_tc7<PREC>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM7_TOTAL));
+        attr = true;
+    }
+    const uint64_t slots = uint64_t(ctx().sm_count);
+    const unsigned grid = (unsigned)(p.ntiles * 4 < slots ? p.ntiles * 4 : slots);
+    k_transmm_tc7<PREC><<<grid, TC_THREADS, SM7_TOTAL, st>>>(p);
+    HQ_CHECK_CUDA(cudaGetLastError());
+}
+
 void launch_transmm_tc(const TransmmLaunch& p, cudaStream_t st) {
-    HQ_REQUIRE(p.m == 6 && p.k == TC_TILE_BITS, HQ_ERR_UNSUPPORTED,
-               "tensor-core TransMM runs 6-qubit groups on 13-qubit tiles");
-    if (p.precision == HQ_MM_TF32)
+    HQ_REQUIRE((p.m == 6 || p.m == 7) && p.k == TC_TILE_BITS, HQ_ERR_UNSUPPORTED,
+               "tensor-core TransMM runs 6- and 7-qubit groups on 13-qubit tiles");
+    if (p.m == 7) {
+        if (p.precision == HQ_MM_TF32)
+            launch_prec7<HQ_MM_TF32>(p, st);
+        else
+            launch_prec7<HQ_MM_BF16X3>(p, st);
+    } else if (p.precision == HQ_MM_TF32) {
         launch_prec<HQ_MM_TF32>(p, st);
-    else
+    } else {
         launch_prec<HQ_MM_BF16X3>(p, st);
+    }
 }
 
 }  // namespace hq

@@ -185,7 +185,7 @@ void launch_transmm_simt(const TransmmLaunch& p, cudaStream_t st) {
 
 // group widths each contraction runs (narrower groups are padded with idle qubits)
 static int min_mm_qubits(int precision) { return precision == HQ_MM_FP32 ? 4 : 6; }
-static int max_mm_qubits(int precision) { return precision == HQ_MM_FP32 ? 7 : 6; }
+static int max_mm_qubits(int) { return 7; }
 
 // Rows = the group's qubits padded up to the kernel's minimum with the lowest
 // free physical qubits; tile = rows + lowest non-row qubits up to 13 bits.
@@ -271,22 +271,30 @@ static TransmmLaunch make_launch(int n, int m, uint64_t rows, uint64_t tile, int
         p.piece_off[mm] = off;
         p.piece_slot[mm] = tile_swz(local);
     }
-    // sub-tiles for the tensor-core kernel (6 row bits + 7 column bits): the top
-    // column bit splits the tile
-    if (m == 6) {
-        const int split = p.col_local[6];
+    // sub-tiles for the tensor-core kernels: m = 6 (7 column bits) fixes the top
+    // column bit (64 x 64 sub-tiles), m = 7 (6 column bits) the top two (128 x 16)
+    if (m == 6 || m == 7) {
+        const int ncol = kSimtK - m, nsplit = m == 6 ? 1 : 2;
+        const int sub_bits = kSimtK - nsplit;
         int sub[16];
-        for (int j = 0, q = 0; j < kSimtK; j++) {
-            sub[j] = j == split ? -1 : q;
-            if (j != split) p.sub_phys[q++] = p.tile_phys[j];
+        for (int j = 0; j < kSimtK; j++) sub[j] = 0;
+        bool fixed[16] = {false};
+        for (int f = 0; f < nsplit; f++) {
+            const int j = p.col_local[ncol - nsplit + f];
+            fixed[j] = true;
+            p.split_off[f] = uint64_t(1) << p.tile_phys[j];
         }
-        for (int r = 0; r < 6; r++) p.row_sub[r] = (uint8_t)sub[p.row_local[r]];
-        for (int c = 0; c < 6; c++) p.col_sub[c] = (uint8_t)sub[p.col_local[c]];
-        p.split_off = uint64_t(1) << p.tile_phys[split];
-        for (int mm = 0; mm < 8; mm++) {
+        for (int j = 0, q = 0; j < kSimtK; j++) {
+            sub[j] = fixed[j] ? -1 : q;
+            if (!fixed[j]) p.sub_phys[q++] = p.tile_phys[j];
+        }
+        for (int r = 0; r < m; r++) p.row_sub[r] = (uint8_t)sub[p.row_local[r]];
+        for (int c = 0; c < ncol - nsplit; c++) p.col_sub[c] = (uint8_t)sub[p.col_local[c]];
+        const int ppt = (1 << (sub_bits - 1)) / 256;
+        for (int mm = 0; mm < ppt; mm++) {
             const uint32_t local = uint32_t(2 * mm * 256);
             uint64_t off = 0;
-            for (int j = 0; j < kSimtK - 1; j++)
+            for (int j = 0; j < sub_bits; j++)
                 if ((local >> j) & 1) off |= uint64_t(1) << p.sub_phys[j];
             p.sub_piece_off[mm] = off;
             p.sub_piece_slot[mm] = tile_swz(local);

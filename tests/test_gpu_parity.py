@@ -194,7 +194,8 @@ MM_TOL = {"fp32": (TOL, FID), "bf16x3": (TOL, FID), "tf32": (5e-5, 1e-5)}
 
 
 @pytest.mark.parametrize("prec,m", [("fp32", 4), ("fp32", 5), ("fp32", 6), ("fp32", 7),
-                                    ("bf16x3", 4), ("bf16x3", 6), ("tf32", 6)])
+                                    ("bf16x3", 4), ("bf16x3", 6), ("tf32", 6), ("bf16x3", 7),
+                                    ("tf32", 7)])
 def test_transmm_single_group(hq, oracle, prec, m):
     n = 17
     rng = W.SplitMix64(900 + m)
@@ -223,16 +224,17 @@ def test_apply_caller_unitary_narrow_group(hq, oracle, prec):
     check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
 
 
-@pytest.mark.parametrize("prec", ["bf16x3", "tf32", "fp32"])
-def test_transmm_qft_precision_sweep(hq, oracle, prec):
+@pytest.mark.parametrize("prec,k", [("bf16x3", 6), ("tf32", 6), ("fp32", 6), ("bf16x3", 7),
+                                    ("tf32", 7), ("fp32", 7)])
+def test_transmm_qft_precision_sweep(hq, oracle, prec, k):
     """Config-3 shape at a size the oracle finishes: QFT on a random state,
-    TransMM groups only, per arithmetic."""
+    TransMM groups of k qubits only, per arithmetic."""
     n = 18
     desc = W.qft(n)
     psi = W.random_state(31, n)
     c = hq.Circuit(n)
     c.addGates(W.to_gates(desc))
-    c.compile(backend="transmm", precision=prec, mm_qubits=6)
+    c.compile(backend="transmm", precision=prec, mm_qubits=k)
     s = hq.State(n, zero=False)
     s.load(psi)
     c.run_on(s)
