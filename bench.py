@@ -336,7 +336,7 @@ def base_line(args, dist, metric, value, unit, ms, hib, workload, extra_cfg=None
 
 
 def run_plain20(args, dist: Dist):
-    """Config 1: 20 qubits, plain gate-by-gate path, |0..0>, full state out."""
+    """20 qubits, plain gate-by-gate path, |0..0>, full state out."""
     import hyquas_gb300 as hq
     from hyquas_gb300 import workloads as W
     import oracle as O
@@ -416,7 +416,7 @@ def run_plain20(args, dist: Dist):
 
 
 def run_qft28(args, dist: Dist):
-    """Config 3: QFT-28 precision sweep on a seeded random state."""
+    """QFT-28 precision sweep on a seeded random state."""
     import hyquas_gb300 as hq
     from hyquas_gb300 import workloads as W
     hq.init(dist.local)
@@ -481,7 +481,7 @@ def run_qft28(args, dist: Dist):
 
 
 def run_batch(args, dist: Dist):
-    """Config 4: 512 circuits in one persistent launch vs each alone."""
+    """512 circuits in one persistent launch vs each alone."""
     import hyquas_gb300 as hq
     from hyquas_gb300 import workloads as W
     import oracle as O
@@ -569,7 +569,7 @@ def run_batch(args, dist: Dist):
 
 
 def run_serve(args, dist: Dist):
-    """Config 5: Poisson streams through the request loop."""
+    """Poisson streams of circuits through the request loop."""
     import hyquas_gb300 as hq
     from hyquas_gb300 import workloads as W
     hq.init(dist.local)

@@ -59,7 +59,7 @@ def g2(t, c, q, *params):
 
 
 def plain_u3_cnot(seed: int = 1, n: int = 20, layers: int = 10):
-    """Config 1: per layer U3(theta, phi, lambda) on every qubit with angles
+    """The 20-qubit plain-path circuit: per layer U3(theta, phi, lambda) on every qubit with angles
     uniform in [0, 2pi), then CNOT on a random perfect matching."""
     rng = SplitMix64(seed)
     gates = []
@@ -85,7 +85,7 @@ def grid_couplers(rows: int, cols: int):
 
 
 def grid_random(seed: int = 2, rows: int = 5, cols: int = 6, cycles: int = 20):
-    """Config 2: per cycle a random sqrt(X) / sqrt(Y) / T on every qubit (never
+    """The random grid circuit: per cycle a random sqrt(X) / sqrt(Y) / T on every qubit (never
     the gate that qubit had in the previous cycle), then CZ on the cycle's
     coupler pattern (4 patterns, alternating).  sqrt(X) = RX(pi/2) and sqrt(Y) =
     RY(pi/2) with the reference's RX/RY matrices."""
@@ -111,7 +111,7 @@ def grid_random(seed: int = 2, rows: int = 5, cols: int = 6, cycles: int = 20):
 
 
 def qft(n: int = 28, swaps: bool = True):
-    """Config 3: H and CU1(pi / 2^k) for all n(n-1)/2 pairs, then the final
+    """The quantum Fourier transform: H and CU1(pi / 2^k) for all n(n-1)/2 pairs, then the final
     qubit-order swaps (as SWAP gates, folded into the layout)."""
     gates = []
     for j in range(n - 1, -1, -1):
@@ -134,7 +134,7 @@ def random_state(seed: int, n: int) -> np.ndarray:
 
 
 def ry_rz_cz(rng: SplitMix64, n: int, depth: int):
-    """Config 4/5 circuit body: per layer RY and RZ (angles in [0, 2pi)) on every
+    """The batched and served circuit body: per layer RY and RZ (angles in [0, 2pi)) on every
     qubit, then CZ on a random perfect matching."""
     gates = []
     for _ in range(depth):
@@ -149,7 +149,7 @@ def ry_rz_cz(rng: SplitMix64, n: int, depth: int):
 
 def batched(seed: int = 4, count: int = 512, nmin: int = 10, nmax: int = 22, dmin: int = 8,
             dmax: int = 40):
-    """Config 4: `count` circuits, n uniform in [nmin, nmax], depth uniform in [dmin, dmax]."""
+    """A batch of `count` circuits, n uniform in [nmin, nmax], depth uniform in [dmin, dmax]."""
     rng = SplitMix64(seed)
     out = []
     for _ in range(count):
@@ -161,8 +161,8 @@ def batched(seed: int = 4, count: int = 512, nmin: int = 10, nmax: int = 22, dmi
 
 def served_stream(seed: int = 5, count: int = 200, rate: float = 1000.0, nmin: int = 12,
                   nmax: int = 32, dmin: int = 10, dmax: int = 60):
-    """Config 5: Poisson arrivals at `rate` per second; n log-uniform in
-    [nmin, nmax]; circuits as in config 4.  Returns (arrival_s, n, gates)."""
+    """A served stream: Poisson arrivals at `rate` per second; n log-uniform in
+    [nmin, nmax]; circuits as in the batch.  Returns (arrival_s, n, gates)."""
     rng = SplitMix64(seed)
     t = 0.0
     out = []

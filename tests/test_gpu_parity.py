@@ -1,6 +1,6 @@
 """GPU parity: every CUDA path against the FP64 oracle (and the reference's own
 fused-unitary outputs in tests/golden).  Tolerance for the complex64 state:
-max |d amp| <= 1e-5 and 1 - fidelity <= 1e-6 (the spec error bar)."""
+max |d amp| <= 1e-5 and 1 - fidelity <= 1e-6."""
 import json
 import math
 from pathlib import Path
@@ -227,7 +227,7 @@ def test_apply_caller_unitary_narrow_group(hq, oracle, prec):
 @pytest.mark.parametrize("prec,k", [("bf16x3", 6), ("tf32", 6), ("fp32", 6), ("bf16x3", 7),
                                     ("tf32", 7), ("fp32", 7)])
 def test_transmm_qft_precision_sweep(hq, oracle, prec, k):
-    """Config-3 shape at a size the oracle finishes: QFT on a random state,
+    """The QFT precision sweep at a size the oracle finishes: QFT on a random state,
     TransMM groups of k qubits only, per arithmetic."""
     n = 18
     desc = W.qft(n)
@@ -255,7 +255,7 @@ def inverse(desc):
 
 
 def test_grid30_oshm_vs_plain_full_size(hq, oracle):
-    """Config 2 at full size (8 GiB): the OShareMem schedule and the plain
+    """The 30-qubit grid circuit at full size (8 GiB): the OShareMem schedule and the plain
     per-gate path are independent CUDA paths; they must agree, and the state
     must stay normalised."""
     n = 30
