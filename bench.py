@@ -23,8 +23,8 @@ ms_per_step is device time per circuit.
                 cores, on a bounded sample (the circuit's first gates), scaled
                 to circuits/s.
   --impl reference   the same CPU port as the reference arm (the reference
-                has no CPU implementation of the path; its GPU build needs
-                sources that are not on the GPU machine).
+                has no CPU implementation of the path, and it is a CMake
+                C++/CUDA project that does not install as a package).
 
 The other workloads print one line each with their own metric:
   plain20  20 qubits, 10 layers of U3 on every qubit + CNOT matching, plain
