@@ -70,7 +70,8 @@ void batch_compile(hq_batch_s* b, const hq_compile_options* opt) {
     for (BatchEntry& e : b->entries) {
         const int n = e.n;
         std::vector<int> perm;
-        e.folded = fold_swaps(e.gates, n, perm);
+        // the batched kernel interprets its ops: fewer, fused ops run faster
+        e.folded = fuse_single_qubit_runs(fold_swaps(e.gates, n, perm), n);
         e.swap_perm = perm;
         e.group0 = (uint32_t)progs.size();
         e.ngroups = 0;

@@ -138,4 +138,39 @@ std::vector<hq_gate> fold_swaps(const std::vector<hq_gate>& gates, int n, std::v
     return out;
 }
 
+// Consecutive single-qubit gates on one qubit (no gate touching that qubit in
+// between) multiplied into one 2x2 gate, kept where the first of them stood.
+std::vector<hq_gate> fuse_single_qubit_runs(const std::vector<hq_gate>& gates, int n) {
+    std::vector<hq_gate> out;
+    std::vector<int> open(n, -1);  // qubit -> index in `out` of a 1q gate still open for fusion
+    for (const hq_gate& g : gates) {
+        const bool one = g.control < 0 && g.control2 < 0 && g.type != G_SWAP;
+        if (one && open[g.target] >= 0) {
+            hq_gate& f = out[open[g.target]];
+            // f <- g . f (g acts after f)
+            double m[8];
+            for (int r = 0; r < 2; r++)
+                for (int c = 0; c < 2; c++) {
+                    double re = 0, im = 0;
+                    for (int k = 0; k < 2; k++) {
+                        const double ar = g.mat[(r * 2 + k) * 2], ai = g.mat[(r * 2 + k) * 2 + 1];
+                        const double br = f.mat[(k * 2 + c) * 2], bi = f.mat[(k * 2 + c) * 2 + 1];
+                        re += ar * br - ai * bi;
+                        im += ar * bi + ai * br;
+                    }
+                    m[(r * 2 + c) * 2] = re;
+                    m[(r * 2 + c) * 2 + 1] = im;
+                }
+            for (int q = 0; q < 8; q++) f.mat[q] = m[q];
+            f.type = G_U3;  // a general single-qubit matrix (the planner reads the matrix)
+            continue;
+        }
+        for (uint64_t qs = gate_qubits(g); qs; qs &= qs - 1) open[__builtin_ctzll(qs)] = -1;
+        if (g.type == G_SWAP) open[g.control] = -1;
+        out.push_back(g);
+        if (one) open[g.target] = (int)out.size() - 1;
+    }
+    return out;
+}
+
 }  // namespace hq

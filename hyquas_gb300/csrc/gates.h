@@ -49,6 +49,10 @@ inline uint64_t gate_controls(const hq_gate& g) {
 // all swaps are applied (so the readout layout is pos[s] = layout[perm[s]]).
 std::vector<hq_gate> fold_swaps(const std::vector<hq_gate>& gates, int n, std::vector<int>& perm);
 
+// Runs of single-qubit gates on one qubit multiplied into one gate each (for
+// the interpreted kernels, whose cost is per gate rather than per flop).
+std::vector<hq_gate> fuse_single_qubit_runs(const std::vector<hq_gate>& gates, int n);
+
 // OpenQASM 2 text -> register size and gate list (qasm.cpp).
 void parse_qasm(const char* text, int& n, std::vector<hq_gate>& out);
 

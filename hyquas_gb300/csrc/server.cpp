@@ -66,7 +66,7 @@ bool same_gates(const std::vector<hq_gate>& a, const std::vector<hq_gate>& b) {
 
 void plan_request(Request* r, int fixed_k) {
     std::vector<int> perm;
-    std::vector<hq_gate> folded = fold_swaps(r->gates, r->n, perm);
+    std::vector<hq_gate> folded = fuse_single_qubit_runs(fold_swaps(r->gates, r->n, perm), r->n);
     r->swap_perm = perm;
     const int n = r->n;
     if (folded.empty()) return;
