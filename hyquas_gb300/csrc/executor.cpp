@@ -281,6 +281,15 @@ void circuit_compile(hq_circuit_s* c, const hq_compile_options& o) {
     c->orig_index.clear();
     for (size_t i = 0; i < c->gates.size(); i++)
         if (c->gates[i].type != G_SWAP) c->orig_index.push_back((int)i);
+    if (o.specialize == 0 && o.backend != HQ_BACKEND_PLAIN && !o.reference_grouping) {
+        // interpreted kernels pay per op: fuse runs of single-qubit gates (a
+        // fused gate is listed in its group by its first gate)
+        std::vector<int> origin;
+        c->folded = fuse_single_qubit_runs(c->folded, n, &origin);
+        std::vector<int> idx;
+        for (int x : origin) idx.push_back(c->orig_index[x]);
+        c->orig_index.swap(idx);
+    }
 
     CompileConfig cfg = config_from_options(o, n);
     if (o.backend == HQ_BACKEND_PLAIN || n < 6) {

@@ -140,8 +140,10 @@ std::vector<hq_gate> fold_swaps(const std::vector<hq_gate>& gates, int n, std::v
 
 // Consecutive single-qubit gates on one qubit (no gate touching that qubit in
 // between) multiplied into one 2x2 gate, kept where the first of them stood.
-std::vector<hq_gate> fuse_single_qubit_runs(const std::vector<hq_gate>& gates, int n) {
+std::vector<hq_gate> fuse_single_qubit_runs(const std::vector<hq_gate>& gates, int n,
+                                            std::vector<int>* origin) {
     std::vector<hq_gate> out;
+    if (origin) origin->clear();
     std::vector<int> open(n, -1);  // qubit -> index in `out` of a 1q gate still open for fusion
     for (const hq_gate& g : gates) {
         const bool one = g.control < 0 && g.control2 < 0 && g.type != G_SWAP;
@@ -168,6 +170,7 @@ std::vector<hq_gate> fuse_single_qubit_runs(const std::vector<hq_gate>& gates, i
         for (uint64_t qs = gate_qubits(g); qs; qs &= qs - 1) open[__builtin_ctzll(qs)] = -1;
         if (g.type == G_SWAP) open[g.control] = -1;
         out.push_back(g);
+        if (origin) origin->push_back(int(&g - gates.data()));
         if (one) open[g.target] = (int)out.size() - 1;
     }
     return out;

@@ -51,7 +51,9 @@ std::vector<hq_gate> fold_swaps(const std::vector<hq_gate>& gates, int n, std::v
 
 // Runs of single-qubit gates on one qubit multiplied into one gate each (for
 // the interpreted kernels, whose cost is per gate rather than per flop).
-std::vector<hq_gate> fuse_single_qubit_runs(const std::vector<hq_gate>& gates, int n);
+// origin (optional): for each output gate, the index of its first input gate.
+std::vector<hq_gate> fuse_single_qubit_runs(const std::vector<hq_gate>& gates, int n,
+                                            std::vector<int>* origin = nullptr);
 
 // OpenQASM 2 text -> register size and gate list (qasm.cpp).
 void parse_qasm(const char* text, int& n, std::vector<hq_gate>& out);

@@ -188,9 +188,10 @@ typedef struct hq_compile_options {
     int32_t mm_qubits;     /* TransMM group width (0 = autotuned, else 4..8) */
     int32_t mm_precision;  /* hq_mm_precision */
     int32_t reference_grouping; /* 1 = use the reference's widths (tile 10, coalesce 3, MAT 6) */
-    int32_t specialize;    /* OShareMem kernels: 0 = interpreter, 1 = one generated kernel per
-                              group (NVRTC, error if unavailable), 2 = generated when NVRTC is
-                              present, else interpreter (default) */
+    int32_t specialize;    /* OShareMem kernels: 0 = interpreter (runs of single-qubit gates
+                              on a qubit are fused into one gate first), 1 = one generated
+                              kernel per group (NVRTC, error if unavailable), 2 = generated
+                              when NVRTC is present, else interpreter (default) */
 } hq_compile_options;
 
 hq_status hq_compile_options_default(hq_compile_options* opt);
@@ -207,7 +208,8 @@ hq_status hq_circuit_compile(hq_circuit c, const hq_compile_options* opt);
  * Arrays may be NULL; they must hold num_groups entries otherwise. */
 hq_status hq_circuit_schedule(hq_circuit c, int32_t* num_groups, int32_t* backend,
                               int32_t* gates_per_group, int32_t* width, uint64_t* related);
-/* Gate indices (into the added list) of group g, in execution order. */
+/* Gate indices (into the added list) of group g, in execution order (a
+ * fused run of single-qubit gates is listed by its first gate). */
 hq_status hq_circuit_group_gates(hq_circuit c, int32_t g, int32_t* gate_idx, int32_t cap,
                                  int32_t* count);
 /* Host-only planning (no device needed): partition `num_gates` gates as
