@@ -64,7 +64,8 @@ class hq_cost_params(C.Structure):
 
 class hq_server_options(C.Structure):
     _fields_ = [("hbm_budget", C.c_uint64), ("step_budget_us", C.c_double),
-                ("planner_threads", C.c_int32), ("tile_qubits", C.c_int32)]
+                ("planner_threads", C.c_int32), ("tile_qubits", C.c_int32),
+                ("jit_min_qubits", C.c_int32)]
 
 
 def _load():
@@ -603,9 +604,12 @@ REQ_STATUS = {0: "planning", 1: "queued", 2: "running", 3: "done", 4: "failed"}
 
 
 def server_options(hbm_budget: int | None = None, step_budget_us: float = 0.0,
-                   planner_threads: int = 0, tile_qubits: int = 0) -> hq_server_options:
+                   planner_threads: int = 0, tile_qubits: int = 0,
+                   jit_min_qubits: int = 0) -> hq_server_options:
     o = hq_server_options()
     check(lib.hq_server_options_default(C.byref(o)))
+    if jit_min_qubits:
+        o.jit_min_qubits = jit_min_qubits
     if hbm_budget is not None:
         o.hbm_budget = hbm_budget
     if step_budget_us:
@@ -631,9 +635,10 @@ class Server:
     admitted request's next gate groups)."""
 
     def __init__(self, hbm_budget: int | None = None, step_budget_us: float = 0.0,
-                 planner_threads: int = 0, tile_qubits: int = 0):
+                 planner_threads: int = 0, tile_qubits: int = 0, jit_min_qubits: int = 0):
         self._h = C.c_void_p()
-        o = server_options(hbm_budget, step_budget_us, planner_threads, tile_qubits)
+        o = server_options(hbm_budget, step_budget_us, planner_threads, tile_qubits,
+                           jit_min_qubits)
         check(lib.hq_server_create(C.byref(o), C.byref(self._h)))
         self._n: dict[int, int] = {}
 

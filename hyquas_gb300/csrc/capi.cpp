@@ -571,6 +571,7 @@ hq_status hq_server_options_default(hq_server_options* opt) {
     opt->step_budget_us = 2000.0;
     opt->planner_threads = 4;
     opt->tile_qubits = 0;
+    opt->jit_min_qubits = 0;
     HQ_API_END
 }
 

@@ -64,9 +64,12 @@ bool same_gates(const std::vector<hq_gate>& a, const std::vector<hq_gate>& b) {
            (a.empty() || std::memcmp(a.data(), b.data(), sizeof(hq_gate) * a.size()) == 0);
 }
 
-void plan_request(Request* r, int fixed_k) {
+// fuse: runs of single-qubit gates as one gate (for the interpreted batch
+// kernel; generated kernels run the gates unfused more cheaply)
+void plan_request(Request* r, int fixed_k, bool fuse) {
     std::vector<int> perm;
-    std::vector<hq_gate> folded = fuse_single_qubit_runs(fold_swaps(r->gates, r->n, perm), r->n);
+    std::vector<hq_gate> folded = fold_swaps(r->gates, r->n, perm);
+    if (fuse) folded = fuse_single_qubit_runs(folded, r->n);
     r->swap_perm = perm;
     const int n = r->n;
     if (folded.empty()) return;
@@ -112,10 +115,22 @@ void planner_main(hq_server_s* sv) {
                 r->group_cost = hit->group_cost;
                 r->swap_perm = hit->swap_perm;
                 r->k = hit->k;
+                r->jit = hit->jit;
                 std::lock_guard<std::mutex> lk(sv->cache_mu);
                 sv->cache_hits++;
             } else {
-                plan_request(r, sv->opt.tile_qubits);
+                const int jit_min = sv->opt.jit_min_qubits;
+                const bool use_jit = jit_min > 0 && r->n >= jit_min && jit_available();
+                plan_request(r, sv->opt.tile_qubits, !use_jit);
+                if (use_jit && !r->progs.empty()) {
+                    std::vector<const OshmProgram*> ps;
+                    for (const OshmProgram& pg : r->progs) ps.push_back(&pg);
+                    try {
+                        r->jit = jit_compile_groups(ps);
+                    } catch (const Failure&) {
+                        r->jit.clear();  // the batched interpreter runs it instead
+                    }
+                }
                 auto e = std::make_shared<PlanEntry>();
                 e->n = r->n;
                 e->gates = r->gates;
@@ -123,6 +138,7 @@ void planner_main(hq_server_s* sv) {
                 e->group_cost = r->group_cost;
                 e->swap_perm = r->swap_perm;
                 e->k = r->k;
+                e->jit = r->jit;
                 std::lock_guard<std::mutex> lk(sv->cache_mu);
                 if (!sv->plan_cache.count(key)) {
                     sv->plan_cache[key] = e;
@@ -289,11 +305,24 @@ void enqueue_step(hq_server_s* sv, StepBuf& sb, std::vector<Request*>& newly,
     for (Request* r : members)
         if (r->next < r->progs.size()) working++;
     const double share = sv->opt.step_budget_us / double(std::max<size_t>(working, 1));
+    // requests with generated kernels: whole groups, launched on their own
+    std::vector<std::pair<Request*, uint32_t>> jit_runs;  // (request, groups to run)
     for (size_t i = 0; i < nm; i++) {
         Request* r = members[i];
         const uint32_t total = (uint32_t)r->progs.size();
         g0[i] = g1[i] = r->next;
         if (r->next >= total) continue;
+        if (!r->jit.empty()) {
+            uint32_t e = r->next;
+            double acc = 0;
+            while (e < total && (e == r->next || acc + r->group_cost[e] <= share)) {
+                acc += r->group_cost[e];
+                e++;
+            }
+            jit_runs.push_back({r, e});
+            g1[i] = g0[i];  // no batched items
+            continue;
+        }
         const uint64_t tiles = uint64_t(1) << (r->n - r->k);
         const uint32_t ch = batch_chunk_tiles(tiles, slots);
         const double group_us = r->group_cost[r->next];
@@ -379,6 +408,13 @@ void enqueue_step(hq_server_s* sv, StepBuf& sb, std::vector<Request*>& newly,
     // gate-less requests: |0...0> only
     for (Request* r : members)
         if (r->progs.empty() && r->next == 0) launch_init_zero(r->state->d, r->n, st);
+    // generated kernels: |0...0> before the first group, then whole groups
+    for (auto& jr : jit_runs) {
+        Request* r = jr.first;
+        if (r->next == 0) launch_init_zero(r->state->d, r->n, st);
+        for (uint32_t g = r->next; g < jr.second; g++)
+            jit_launch(r->jit[g], r->state->d, uint64_t(1) << (r->n - r->progs[g].k), st);
+    }
     if (nl) {
         HQ_CHECK_CUDA(cudaMemcpyAsync(sb.d, sb.h, launches_b + items_b, cudaMemcpyHostToDevice, st));
         uint32_t* ctr = (uint32_t*)(sb.d + launches_b + items_b);
@@ -399,10 +435,15 @@ void enqueue_step(hq_server_s* sv, StepBuf& sb, std::vector<Request*>& newly,
     HQ_CHECK_CUDA(cudaEventRecord(sb.ev, st));
     sb.members = members;
     sb.finishing.clear();
+    for (auto& jr : jit_runs) jr.first->next = jr.second;
     for (size_t i = 0; i < nm; i++) {
         Request* r = members[i];
         if (r->first_step < 0) r->first_step = sv->steps;
         r->last_step = sv->steps;
+        if (!r->jit.empty()) {
+            if (r->next == r->progs.size()) sb.finishing.push_back(r);
+            continue;
+        }
         if (partial[i]) {
             const uint64_t tiles = uint64_t(1) << (r->n - r->k);
             r->next_tile = tb[i] < tiles ? tb[i] : 0;

@@ -17,6 +17,7 @@
 #include "compiler.h"
 #include "device.h"
 #include "executor.h"
+#include "jit.h"
 
 namespace hq {
 
@@ -29,6 +30,7 @@ struct Request {
     std::vector<double> group_cost;  // estimated device microseconds per group
     std::vector<int> swap_perm;
     int k = 0;
+    std::vector<JitKernel> jit;      // generated group kernels (large requests), else empty
     // device (engine thread)
     hq_state_s* state = nullptr;
     char* d_prog = nullptr;
@@ -54,6 +56,7 @@ struct PlanEntry {
     std::vector<double> group_cost;
     std::vector<int> swap_perm;
     int k = 0;
+    std::vector<JitKernel> jit;
 };
 constexpr size_t kPlanCacheEntries = 256;
 

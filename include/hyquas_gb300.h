@@ -316,8 +316,15 @@ typedef struct hq_server_options {
                                 over its share runs a slice of that group's tiles (0 = 2000) */
     int32_t planner_threads; /* 0 = 4 */
     int32_t tile_qubits;     /* 0 = 13 (or n when smaller); else 10..13 */
+    int32_t jit_min_qubits;  /* requests of at least this many qubits get generated group
+                                kernels (compiled by the planner threads while other work
+                                runs) and run them between the batched launches; 0 or
+                                > 34 = never.  Pays off when circuits repeat (the plan
+                                cache keeps their kernels): compiling a group costs about
+                                a CPU-second, more than it saves on one run */
 } hq_server_options;
-/* Defaults: 150 GB budget, 2000 us steps, 4 planners, tile 13. */
+/* Defaults: 150 GB budget, 2000 us steps, 4 planners, tile 13, no generated
+ * kernels. */
 hq_status hq_server_options_default(hq_server_options* opt);
 /* Host-only admission checks of a request (qubit range 10..34, gate indices,
  * state bytes against the budget); the checks hq_server_submit makes. */

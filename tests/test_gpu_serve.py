@@ -159,3 +159,18 @@ def test_plan_cache_reuses_plans(hq, oracle):
     assert np.array_equal(a, b)
     check(oracle, oracle.run_f64(16, desc), b)
     sv.close()
+
+
+def test_generated_kernel_lane(hq, oracle):
+    """Requests at or above jit_min_qubits run generated group kernels between
+    the batched launches; their results match the oracle and the small
+    requests served beside them."""
+    rng = W.SplitMix64(131)
+    circuits = [(n, W.ry_rz_cz(rng, n, 8 + rng.below(8))) for n in [12, 16, 15, 17, 13, 16]]
+    sv = hq.Server(jit_min_qubits=15)
+    arrays = [hq.gate_array(W.to_gates(d)) for _, d in circuits]
+    ids = [sv.submit(n, a) for (n, _), a in zip(circuits, arrays)]
+    got = drain(sv, ids, timeout=300.0)
+    for rid, (n, d) in zip(ids, circuits):
+        check(oracle, oracle.run_f64(n, d), got[rid])
+    sv.close()
