@@ -93,6 +93,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
     return false;
 }
 
+// The group's A operand (contiguous, a multiple of 16 KB) copied to shared
+// memory by the TMA engine: one thread arms the mbarrier at s_bar with the
+// byte count and issues bulk copies that complete on it.
+__device__ __forceinline__ void bulk_load(uint32_t sdst, const void* gsrc, uint32_t bytes,
+                                          uint32_t s_bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(s_bar), "r"(bytes)
+                 : "memory");
+    for (uint32_t off = 0; off < bytes; off += 16384u)
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                sdst + off),
+            "l"(reinterpret_cast<const char*>(gsrc) + off), "r"(16384u), "r"(s_bar)
+            : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
@@ -158,8 +173,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
     if (t == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar + 8));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar + 24));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
+    __syncthreads();
+    // the group's A operand (prepared once per circuit), 64 KB, by the TMA engine
+    if (t == 0) bulk_load(sb + SM_A, p.umat, 65536u, s_mbar + 24);
     for (int r = t; r < TC_ROWS; r += TC_THREADS) {
         uint32_t x = 0;
         for (int b = 0; b < 6; b++)
@@ -172,15 +191,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
             if ((c >> b) & 1) x |= 1u << p.col_sub[b];
         colslot[c] = tile_swz(x);
     }
-    // the group's A operand (prepared once per circuit), 64 KB
-    const char* asrc = reinterpret_cast<const char*>(p.umat);
-    for (int i = t; i < 4096; i += TC_THREADS) cp_async16(sb + SM_A + i * 16u, asrc + i * 16);
-    cp_async_commit();
-    cp_async_wait_all();
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    const bool a_ok = mbar_wait(s_mbar + 24, 0);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
+    const bool a_failed = __syncthreads_or(!a_ok);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (a_failed && t == 0 && p.err) {
+        atomicCAS(p.err, 0, 1);
+        p.err[1] = 9;  // site: TransMM operand load
+    }
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + SM_MISC + 16);
 
     const uint64_t toff = local_to_phys(uint32_t(t) << 1, TC_TILE_BITS - 1, p.sub_phys);
@@ -210,7 +228,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
         cp_async_commit();
     };
     // results of sub-tile j: TMEM acc[j&1] -> over its staging buffer -> HBM
-    bool failed = false;
+    bool failed = a_failed;
     auto epilogue = [&](uint64_t j) {
         const uint32_t b = uint32_t(j & 1);
         const bool ok = mbar_wait(s_mbar + 8 * b, uint32_t((j >> 1) & 1));
@@ -245,8 +263,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
         __syncthreads();
     };
 
-    load(0);
-    load(1);
+    if (!failed) {
+        load(0);
+        load(1);
+    }
     for (uint64_t j = 0; j < J && !failed; j++) {
         asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         __syncthreads();
@@ -338,6 +358,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
     }
     if (!failed && J > 0) epilogue(J - 1);
     cp_async_wait_all();
+    if (a_failed) mbar_wait(s_mbar + 24, 0);  // the operand copies still in flight, bounded
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));
@@ -382,8 +403,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc7(const TransmmLaun
     if (t == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar + 8));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar + 24));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
+    __syncthreads();
+    if (t == 0) bulk_load(sb + SM7_A, p.umat, 131072u, s_mbar + 24);  // Ur, Ui: 128 KB
     for (int r = t; r < T7_ROWS; r += TC_THREADS) {
         uint32_t x = 0;
         for (int b = 0; b < 7; b++)
@@ -396,14 +420,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc7(const TransmmLaun
             if ((c >> b) & 1) x |= 1u << p.col_sub[b];
         colslot[c] = tile_swz(x);
     }
-    const char* asrc = reinterpret_cast<const char*>(p.umat);
-    for (int i = t; i < 8192; i += TC_THREADS) cp_async16(sb + SM7_A + i * 16u, asrc + i * 16);
-    cp_async_commit();
-    cp_async_wait_all();
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    const bool a_ok = mbar_wait(s_mbar + 24, 0);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
+    const bool a_failed = __syncthreads_or(!a_ok);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (a_failed && t == 0 && p.err) {
+        atomicCAS(p.err, 0, 1);
+        p.err[1] = 9;  // site: TransMM operand load
+    }
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + SM7_MISC + 16);
 
     const uint64_t toff = local_to_phys(uint32_t(t) << 1, TC_TILE_BITS - 2, p.sub_phys);
@@ -434,7 +458,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc7(const TransmmLaun
         }
         cp_async_commit();
     };
-    bool failed = false;
+    bool failed = a_failed;
     // results of sub-tile j: (Cr, Ci) in TMEM columns 32 (j&1) and + 16 -> staging -> HBM
     auto epilogue = [&](uint64_t j) {
         const uint32_t b = uint32_t(j & 1);
@@ -472,8 +496,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc7(const TransmmLaun
         __syncthreads();
     };
 
-    load(0);
-    load(1);
+    if (!failed) {
+        load(0);
+        load(1);
+    }
     for (uint64_t j = 0; j < J && !failed; j++) {
         asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         __syncthreads();
@@ -574,6 +600,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc7(const TransmmLaun
     }
     if (!failed && J > 0) epilogue(J - 1);
     cp_async_wait_all();
+    if (a_failed) mbar_wait(s_mbar + 24, 0);  // the operand copies still in flight, bounded
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM7_COLS));
