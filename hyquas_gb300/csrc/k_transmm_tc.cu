@@ -651,22 +651,383 @@ __global__ void k_u_to_tc(const double2* __restrict__ U, unsigned char* __restri
     }
 }
 
+
+// ---- 8-qubit groups ---------------------------------------------------------
+// U (256 x 256 complex) as split BF16 or TF32 is 512 KB, more than shared
+// memory: it streams from L2 (every CTA reads the same 512 KB) through a ring
+// of three 32 KB chunks, each the Ur or Ui block of one 128-row half m of the
+// output over a 64-wide K slice s.  A sub-tile is 256 rows x 16 columns
+// (32 KB, the tile's top column bit fixed); per half m the complex product
+// runs as four real GEMMs (M = 128, N = 16, K = 256 in four slices):
+//     Cr(m) = Ur(m,:).Br + Ui(m,:).(-Bi),   Ci(m) = Ui(m,:).Br + Ur(m,:).Bi
+// Warp-specialised: warps 0-7 stage sub-tiles (cp.async), build B = Br | Bi |
+// -Bi and run the epilogue; warp 8 (one thread) streams the A chunks with bulk
+// copies and issues the MMAs.  Handshakes: bfull (B of sub-tile j written,
+// 256 arrivals), acc[j&1] (MMAs of j complete, tcgen05.commit), afull/aempty
+// per ring slot (bulk-copy bytes landed / the MMAs reading the slot complete).
+constexpr int T8_ROWS = 256;
+constexpr int T8_NSUB = 16;
+constexpr int T8_WORKERS = 256;
+constexpr int T8_THREADS = T8_WORKERS + 32;
+constexpr uint32_t SUB8_BYTES = 32768;  // a sub-tile, float2[4096]
+constexpr uint32_t SM8_R = 0;           // two staging buffers of 32 KB
+constexpr uint32_t SM8_B = 65536;       // Br | Bi | -Bi
+constexpr uint32_t B8_COMP = 16384;
+constexpr uint32_t SM8_A = SM8_B + 3 * B8_COMP;  // ring of A chunks
+constexpr uint32_t A8_CHUNK = 32768;
+constexpr int A8_SLOTS = 3;
+constexpr int A8_CHUNKS = 16;  // per sub-tile, chunk c = (m * 4 + s) * 2 + (0: Ur, 1: Ui)
+constexpr uint32_t SM8_MISC = SM8_A + A8_SLOTS * A8_CHUNK;
+constexpr uint32_t SM8_TOTAL = SM8_MISC + 2048;
+constexpr uint32_t TMEM8_COLS = 128;  // two buffers x (Cr0, Ci0, Cr1, Ci1) x 16 columns
+static_assert(SM8_TOTAL <= 232448, "shared memory per block");
+
+// bar.sync / bar.red over the 256 worker threads only (barrier 1)
+__device__ __forceinline__ void workers_sync() { asm volatile("bar.sync 1, 256;\n" ::: "memory"); }
+__device__ __forceinline__ bool workers_any(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.or.pred p, 1, 256, q;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void set_err(int* err, int site, uint64_t detail) {
+    if (err) {
+        atomicCAS(err, 0, 1);
+        err[1] = site;
+        err[2] = (int)(detail & 0x7fffffff);
+    }
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(T8_THREADS, 1) k_transmm_tc8(const TransmmLaunch p) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    uint32_t* rowslot = reinterpret_cast<uint32_t*>(smem + SM8_MISC + 256);
+    uint32_t* colslot = rowslot + T8_ROWS;
+    const uint32_t sb = smem_u32(smem);
+    const uint32_t m_bfull = sb + SM8_MISC, m_acc = m_bfull + 8, m_afull = m_bfull + 24,
+                   m_aempty = m_bfull + 48, m_fin = m_bfull + 72, s_tslot = m_bfull + 80;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    float2* __restrict__ state = reinterpret_cast<float2*>(p.state);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_tslot),
+                     "r"(TMEM8_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(m_bfull), "r"(T8_WORKERS));
+        for (int i = 0; i < 2; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(m_acc + 8 * i));
+        for (int i = 0; i < A8_SLOTS; i++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(m_afull + 8 * i));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(m_aempty + 8 * i));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(m_fin));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    for (int r = t; r < T8_ROWS; r += T8_THREADS) {
+        uint32_t x = 0;
+        for (int b = 0; b < 8; b++)
+            if ((r >> b) & 1) x |= 1u << p.row_sub[b];
+        rowslot[r] = tile_swz(x);
+    }
+    for (int c = t; c < T8_NSUB; c += T8_THREADS) {
+        uint32_t x = 0;
+        for (int b = 0; b < 4; b++)
+            if ((c >> b) & 1) x |= 1u << p.col_sub[b];
+        colslot[c] = tile_swz(x);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + SM8_MISC + 80);
+
+    constexpr uint32_t esize = PREC == HQ_MM_TF32 ? 4 : 2;
+    const uint64_t nsub = p.ntiles * 2;
+    const uint64_t G = gridDim.x;
+    const uint64_t J = blockIdx.x < nsub ? (nsub - blockIdx.x + G - 1) / G : 0;
+
+    if (warp == T8_WORKERS / 32) {
+        // ---- A stream + MMA issue (one thread) ----
+        if (lane == 0 && J > 0) {
+            constexpr uint32_t sbo_a = (64 / (16 / esize)) * 128;   // A chunk: 128 rows x 64 K
+            constexpr uint32_t sbo_b = (256 / (16 / esize)) * 128;  // B: 16 rows x 256 K
+            constexpr uint32_t slice_b = (64 / (16 / esize)) * 128; // B offset of one K slice
+            constexpr uint32_t a_lo = 16384;                        // A chunk lo half (BF16x3)
+            constexpr uint32_t b_lo = 8192;                         // B component lo half
+            constexpr uint32_t idesc = make_idesc(PREC == HQ_MM_TF32 ? 2u : 1u, 128, T8_NSUB);
+            constexpr int nsteps = PREC == HQ_MM_TF32 ? 8 : 4;      // 32 bytes of K per MMA
+            const char* umat = reinterpret_cast<const char*>(p.umat);
+            auto gemm = [&](uint32_t d, uint32_t a, uint32_t bm, bool first) {
+                if (PREC == HQ_MM_TF32) {
+                    for (int kk = 0; kk < nsteps; kk++)
+                        mma_tf32(d, make_desc(a + kk * 256, 128, sbo_a), make_desc(bm + kk * 256, 128, sbo_b),
+                                 idesc, !first || kk > 0);
+                } else {
+                    for (int kk = 0; kk < nsteps; kk++)  // hi . hi
+                        mma_f16(d, make_desc(a + kk * 256, 128, sbo_a), make_desc(bm + kk * 256, 128, sbo_b),
+                                idesc, !first || kk > 0);
+                    for (int kk = 0; kk < nsteps; kk++)  // hi . lo
+                        mma_f16(d, make_desc(a + kk * 256, 128, sbo_a),
+                                make_desc(bm + b_lo + kk * 256, 128, sbo_b), idesc, 1);
+                    for (int kk = 0; kk < nsteps; kk++)  // lo . hi
+                        mma_f16(d, make_desc(a + a_lo + kk * 256, 128, sbo_a),
+                                make_desc(bm + kk * 256, 128, sbo_b), idesc, 1);
+                }
+            };
+            const uint64_t total = J * A8_CHUNKS;
+            uint64_t issued = 0, consumed = 0;
+            auto fetch = [&](uint64_t h) {
+                const uint32_t slot = uint32_t(h % A8_SLOTS);
+                bulk_load(sb + SM8_A + slot * A8_CHUNK, umat + (h % A8_CHUNKS) * A8_CHUNK, A8_CHUNK,
+                          m_afull + 8 * slot);
+                issued = h + 1;
+            };
+            fetch(0);
+            if (total > 1) fetch(1);
+            bool ok = true;
+            for (uint64_t j = 0; j < J && ok; j++) {
+                if (!mbar_wait(m_bfull, uint32_t(j & 1))) {
+                    set_err(p.err, 10, j);  // site: TransMM operand B handshake
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t accb = tmem + 64 * uint32_t(j & 1);
+                for (int c = 0; c < A8_CHUNKS; c++) {
+                    const uint64_t g = j * A8_CHUNKS + c;
+                    const uint32_t slot = uint32_t(g % A8_SLOTS);
+                    if (!mbar_wait(m_afull + 8 * slot, uint32_t((g / A8_SLOTS) & 1))) {
+                        set_err(p.err, 9, g);  // site: TransMM operand load
+                        ok = false;
+                        break;
+                    }
+                    consumed = g + 1;
+                    const int m = c >> 3, s = (c >> 1) & 3, part = c & 1;
+                    const uint32_t a = sb + SM8_A + slot * A8_CHUNK;
+                    const uint32_t dr = accb + 32 * m, di = dr + 16;
+                    const uint32_t br = sb + SM8_B + s * slice_b, bi = br + B8_COMP, bn = br + 2 * B8_COMP;
+                    if (part == 0) {
+                        gemm(dr, a, br, s == 0);
+                        gemm(di, a, bi, s == 0);
+                    } else {
+                        gemm(dr, a, bn, false);
+                        gemm(di, a, br, false);
+                    }
+                    asm volatile(
+                        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                            m_aempty + 8 * slot)
+                        : "memory");
+                    // refill: chunk g + 2 goes where chunk g - 1 was, once its MMAs completed
+                    const uint64_t h = g + 2;
+                    if (h < total) {
+                        if (h >= A8_SLOTS &&
+                            !mbar_wait(m_aempty + 8 * uint32_t(h % A8_SLOTS), uint32_t(((h - A8_SLOTS) / A8_SLOTS) & 1))) {
+                            set_err(p.err, 9, h);
+                            ok = false;
+                            break;
+                        }
+                        fetch(h);
+                    }
+                }
+                if (!ok) break;
+                asm volatile(
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                        m_acc + 8 * uint32_t(j & 1))
+                    : "memory");
+            }
+            // drain: every issued MMA complete, every issued copy landed (bounded)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             m_fin)
+                         : "memory");
+            mbar_wait(m_fin, 0);
+            for (uint64_t h = consumed; h < issued; h++)
+                mbar_wait(m_afull + 8 * uint32_t(h % A8_SLOTS), uint32_t((h / A8_SLOTS) & 1));
+        }
+        __syncwarp();
+    } else {
+        // ---- workers: staging, B, epilogue ----
+        const uint64_t toff = local_to_phys(uint32_t(t) << 1, TC_TILE_BITS - 1, p.sub_phys);
+        const uint32_t tsl = tile_swz(uint32_t(t) << 1);
+        auto sub_base = [&](uint64_t j) {
+            const uint64_t v = blockIdx.x + j * G;
+            return tile_base(v >> 1, p.nruns, p.run_src, p.run_dst, p.run_len) + (v & 1) * p.split_off[0];
+        };
+        auto load = [&](uint64_t j) {
+            if (j < J) {
+                const float2* gsrc = state + sub_base(j) + toff;
+                const uint32_t rb = sb + SM8_R + uint32_t(j & 1) * SUB8_BYTES;
+#pragma unroll
+                for (int m = 0; m < 8; m++)
+                    cp_async16(rb + (tsl ^ p.sub_piece_slot[m]) * 8u, gsrc + p.sub_piece_off[m]);
+            }
+            cp_async_commit();
+        };
+        // results of sub-tile j: TMEM buffer j&1 -> over its staging buffer -> HBM
+        auto epilogue = [&](uint64_t j) {
+            const uint32_t b = uint32_t(j & 1);
+            float2* Rj = reinterpret_cast<float2*>(smem + SM8_R + b * SUB8_BYTES);
+            const int q = warp & 3, m = warp >> 2;
+            const int i = 128 * m + 32 * q + lane;  // row of the group = TMEM lane 32 q + lane of half m
+            const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + 64 * b + 32 * m;
+            const uint32_t rs = rowslot[i];
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                uint32_t vr[8], vi[8];
+                tmem_ld8(col + 8 * half, vr);
+                tmem_ld8(col + 16 + 8 * half, vi);
+#pragma unroll
+                for (int c = 0; c < 8; c++)
+                    Rj[rs ^ colslot[8 * half + c]] = make_float2(__uint_as_float(vr[c]), __uint_as_float(vi[c]));
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            workers_sync();
+            float2* gdst = state + sub_base(j) + toff;
+            const float4* R4 = reinterpret_cast<const float4*>(Rj);
+#pragma unroll
+            for (int mm = 0; mm < 8; mm++)
+                *reinterpret_cast<float4*>(gdst + p.sub_piece_off[mm]) = R4[(tsl ^ p.sub_piece_slot[mm]) >> 1];
+            workers_sync();
+        };
+        bool failed = false;
+        load(0);
+        for (uint64_t j = 0; j < J; j++) {
+            cp_async_wait_all();  // sub-tile j staged
+            workers_sync();
+            if (j > 0) {  // MMAs of j - 1 complete: B is free, accumulators j - 1 ready
+                const bool ok = mbar_wait(m_acc + 8 * uint32_t((j - 1) & 1), uint32_t(((j - 1) >> 1) & 1));
+                if (workers_any(!ok)) {
+                    if (t == 0) set_err(p.err, 7, j - 1);  // site: TransMM accumulator wait
+                    failed = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            }
+            {
+                const float2* Rj = reinterpret_cast<const float2*>(smem + SM8_R + uint32_t(j & 1) * SUB8_BYTES);
+                unsigned char* B = smem + SM8_B;
+                const int n = t & 15, rb = t >> 4;  // column n, rows 16 rb .. 16 rb + 15
+                const uint32_t cs = colslot[n];
+                float re[16], im[16];
+#pragma unroll
+                for (int qq = 0; qq < 16; qq++) {
+                    const float2 a = Rj[rowslot[rb * 16 + qq] ^ cs];
+                    re[qq] = a.x;
+                    im[qq] = a.y;
+                }
+                if (PREC == HQ_MM_TF32) {
+#pragma unroll
+                    for (int h4 = 0; h4 < 4; h4++) {
+                        const uint32_t o = kmajor_off(n, rb * 16 + 4 * h4, 256, 4);
+                        const float4 vr = make_float4(to_tf32(re[4 * h4]), to_tf32(re[4 * h4 + 1]),
+                                                      to_tf32(re[4 * h4 + 2]), to_tf32(re[4 * h4 + 3]));
+                        const float4 vi = make_float4(to_tf32(im[4 * h4]), to_tf32(im[4 * h4 + 1]),
+                                                      to_tf32(im[4 * h4 + 2]), to_tf32(im[4 * h4 + 3]));
+                        *reinterpret_cast<float4*>(B + o) = vr;
+                        *reinterpret_cast<float4*>(B + B8_COMP + o) = vi;
+                        *reinterpret_cast<float4*>(B + 2 * B8_COMP + o) = make_float4(-vi.x, -vi.y, -vi.z, -vi.w);
+                    }
+                } else {
+                    constexpr uint32_t b_lo = 8192;
+                    const uint32_t sg = 0x80008000u;  // BF16 sign bits: -Bi exactly
+#pragma unroll
+                    for (int h8 = 0; h8 < 2; h8++) {
+                        uint32_t hre[4], lre[4], him[4], lim[4];
+#pragma unroll
+                        for (int qq = 0; qq < 4; qq++) {
+                            const float x0 = re[8 * h8 + 2 * qq], x1 = re[8 * h8 + 2 * qq + 1];
+                            const float y0 = im[8 * h8 + 2 * qq], y1 = im[8 * h8 + 2 * qq + 1];
+                            const __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
+                            const __nv_bfloat16 g0 = __float2bfloat16_rn(y0), g1 = __float2bfloat16_rn(y1);
+                            hre[qq] = pack_bf16(h0, h1);
+                            lre[qq] = pack_bf16(__float2bfloat16_rn(x0 - __bfloat162float(h0)),
+                                                __float2bfloat16_rn(x1 - __bfloat162float(h1)));
+                            him[qq] = pack_bf16(g0, g1);
+                            lim[qq] = pack_bf16(__float2bfloat16_rn(y0 - __bfloat162float(g0)),
+                                                __float2bfloat16_rn(y1 - __bfloat162float(g1)));
+                        }
+                        const uint32_t o = kmajor_off(n, rb * 16 + 8 * h8, 256, 2);
+                        *reinterpret_cast<uint4*>(B + o) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+                        *reinterpret_cast<uint4*>(B + b_lo + o) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
+                        *reinterpret_cast<uint4*>(B + B8_COMP + o) = make_uint4(him[0], him[1], him[2], him[3]);
+                        *reinterpret_cast<uint4*>(B + B8_COMP + b_lo + o) =
+                            make_uint4(lim[0], lim[1], lim[2], lim[3]);
+                        *reinterpret_cast<uint4*>(B + 2 * B8_COMP + o) =
+                            make_uint4(him[0] ^ sg, him[1] ^ sg, him[2] ^ sg, him[3] ^ sg);
+                        *reinterpret_cast<uint4*>(B + 2 * B8_COMP + b_lo + o) =
+                            make_uint4(lim[0] ^ sg, lim[1] ^ sg, lim[2] ^ sg, lim[3] ^ sg);
+                    }
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(m_bfull) : "memory");
+            if (j > 0) epilogue(j - 1);
+            load(j + 1);  // into the buffer sub-tile j - 1 just left
+        }
+        if (!failed && J > 0) {
+            const bool ok = mbar_wait(m_acc + 8 * uint32_t((J - 1) & 1), uint32_t(((J - 1) >> 1) & 1));
+            if (workers_any(!ok)) {
+                if (t == 0) set_err(p.err, 7, J - 1);
+            } else {
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                epilogue(J - 1);
+            }
+        }
+        cp_async_wait_all();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM8_COLS));
+}
+
+// A operand of an 8-qubit group from U (256 x 256, column-major complex128):
+// 16 chunks of 32 KB in the order the kernel consumes them, chunk
+// (m * 4 + s) * 2 + part = Ur (part 0) or Ui (part 1) of rows 128 m .. 128 m + 127
+// and K 64 s .. 64 s + 63, K-major (split BF16 hi at +0 and lo at +16 KB, or TF32).
+__global__ void k_u_to_tc8(const double2* __restrict__ U, unsigned char* __restrict__ out, int prec) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 256 * 256) return;
+    const int r = idx / 256, k = idx % 256;
+    const double2 u = U[(size_t)k * 256 + r];
+    const double v[2] = {u.x, u.y};
+    const int m = r >> 7, rr = r & 127, s = k >> 6, kk = k & 63;
+    for (int part = 0; part < 2; part++) {
+        unsigned char* base = out + size_t((m * 4 + s) * 2 + part) * A8_CHUNK;
+        if (prec == HQ_MM_TF32) {
+            *reinterpret_cast<float*>(base + kmajor_off(rr, kk, 64, 4)) = to_tf32((float)v[part]);
+        } else {
+            const __nv_bfloat16 hi = __float2bfloat16_rn((float)v[part]);
+            const __nv_bfloat16 lo = __float2bfloat16_rn((float)(v[part] - (double)__bfloat162float(hi)));
+            *reinterpret_cast<__nv_bfloat16*>(base + kmajor_off(rr, kk, 64, 2)) = hi;
+            *reinterpret_cast<__nv_bfloat16*>(base + 16384 + kmajor_off(rr, kk, 64, 2)) = lo;
+        }
+    }
+}
+
 }  // namespace
 
 size_t transmm_tc_operand_bytes(int m, int precision) {
     (void)precision;
-    HQ_REQUIRE(m == 6 || m == 7, HQ_ERR_UNSUPPORTED,
-               "tensor-core TransMM runs 6- and 7-qubit groups (got %d)", m);
-    return m == 6 ? 65536 : 131072;
+    HQ_REQUIRE(m >= 6 && m <= 8, HQ_ERR_UNSUPPORTED,
+               "tensor-core TransMM runs 6- to 8-qubit groups (got %d)", m);
+    return m == 6 ? 65536 : m == 7 ? 131072 : size_t(A8_CHUNKS) * A8_CHUNK;
 }
 
 void launch_u_to_tc_operand(int m, int precision, const double* d_u, void* d_out, cudaStream_t st) {
-    HQ_REQUIRE(m == 6 || m == 7, HQ_ERR_UNSUPPORTED,
-               "tensor-core TransMM runs 6- and 7-qubit groups (got %d)", m);
+    HQ_REQUIRE(m >= 6 && m <= 8, HQ_ERR_UNSUPPORTED,
+               "tensor-core TransMM runs 6- to 8-qubit groups (got %d)", m);
     if (m == 6)
         k_u_to_tc<<<64, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
-    else
+    else if (m == 7)
         k_u_to_tc7<<<64, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
+    else
+        k_u_to_tc8<<<256, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -698,10 +1059,29 @@ static void launch_prec7(const TransmmLaunch& p, cudaStream_t st) {
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 
+template <int PREC>
+static void launch_prec8(const TransmmLaunch& p, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        HQ_CHECK_CUDA(cudaFuncSetAttribute(k_transmm_tc8<PREC>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM8_TOTAL));
+        attr = true;
+    }
+    const uint64_t slots = uint64_t(ctx().sm_count);
+    const unsigned grid = (unsigned)(p.ntiles * 2 < slots ? p.ntiles * 2 : slots);
+    k_transmm_tc8<PREC><<<grid, T8_THREADS, SM8_TOTAL, st>>>(p);
+    HQ_CHECK_CUDA(cudaGetLastError());
+}
+
 void launch_transmm_tc(const TransmmLaunch& p, cudaStream_t st) {
-    HQ_REQUIRE((p.m == 6 || p.m == 7) && p.k == TC_TILE_BITS, HQ_ERR_UNSUPPORTED,
-               "tensor-core TransMM runs 6- and 7-qubit groups on 13-qubit tiles");
-    if (p.m == 7) {
+    HQ_REQUIRE(p.m >= 6 && p.m <= 8 && p.k == TC_TILE_BITS, HQ_ERR_UNSUPPORTED,
+               "tensor-core TransMM runs 6- to 8-qubit groups on 13-qubit tiles");
+    if (p.m == 8) {
+        if (p.precision == HQ_MM_TF32)
+            launch_prec8<HQ_MM_TF32>(p, st);
+        else
+            launch_prec8<HQ_MM_BF16X3>(p, st);
+    } else if (p.m == 7) {
         if (p.precision == HQ_MM_TF32)
             launch_prec7<HQ_MM_TF32>(p, st);
         else

@@ -140,6 +140,102 @@ __global__ void __launch_bounds__(kSimtThreads) k_transmm_simt(const TransmmLaun
     for (int i = 0; i < RPT; i++) state[base + rowoff[rg * RPT + i] + coff] = acc[i];
 }
 
+// 8-qubit groups: U (256 x 256 complex, 512 KB) does not fit shared memory, so
+// it streams through two 64 KB buffers of 32 columns (K slices) while the
+// tile (256 rows x 32 columns) stays resident; the thread mapping is the one
+// above with R = 256, C = 32.
+constexpr int kSimt8Slice = 32;
+constexpr size_t kSimt8Smem = (sizeof(float2) << kSimtK) + 2 * sizeof(float2) * kSimt8Slice * 256 +
+                              (sizeof(uint64_t) + sizeof(uint32_t)) * 256;
+
+__global__ void __launch_bounds__(kSimtThreads) k_transmm_simt8(const TransmmLaunch p) {
+    constexpr int K = kSimtK, M = 8, R = 1 << M, C = 1 << (K - M), RPT = 16, KC = kSimt8Slice;
+    static_assert((R / RPT) * C == kSimtThreads, "thread mapping");
+    extern __shared__ float4 smem4[];
+    float2* tile = reinterpret_cast<float2*>(smem4);
+    float2* Ubuf = tile + (1 << K);  // two slices of KC columns
+    uint64_t* rowoff = reinterpret_cast<uint64_t*>(Ubuf + 2 * KC * R);
+    uint32_t* rowslot = reinterpret_cast<uint32_t*>(rowoff + R);
+    const int tid = threadIdx.x;
+    float2* __restrict__ state = reinterpret_cast<float2*>(p.state);
+    const float4* usrc = reinterpret_cast<const float4*>(p.umat);
+    const uint64_t base = tile_base(blockIdx.x, p.nruns, p.run_src, p.run_dst, p.run_len);
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(tile);
+    const uint32_t ubase = (uint32_t)__cvta_generic_to_shared(Ubuf);
+    // slice c = columns c*KC .. c*KC+KC-1 of U (column-major: contiguous)
+    auto stage_slice = [&](int c) {
+        const uint32_t dst = ubase + uint32_t(c & 1) * (KC * R * 8u);
+        const float4* src = usrc + size_t(c) * (KC * R / 2);
+        for (int i = tid; i < KC * R / 2; i += kSimtThreads) cp_async16(dst + i * 16u, src + i);
+    };
+    {
+        const uint64_t toff = local_to_phys(uint32_t(tid) << 1, K, p.tile_phys);
+        const uint32_t tslot = tile_swz(uint32_t(tid) << 1);
+        constexpr int PPT = (1 << (K - 1)) / kSimtThreads;
+#pragma unroll
+        for (int mm = 0; mm < PPT; mm++)
+            cp_async16(sbase + (tslot ^ p.piece_slot[mm]) * 8u, state + base + toff + p.piece_off[mm]);
+    }
+    stage_slice(0);
+    cp_async_commit();
+    for (int r = tid; r < R; r += kSimtThreads) {
+        uint32_t x = 0;
+        uint64_t off = 0;
+        for (int b = 0; b < M; b++)
+            if ((r >> b) & 1) {
+                x |= 1u << p.row_local[b];
+                off |= uint64_t(1) << p.tile_phys[p.row_local[b]];
+            }
+        rowslot[r] = tile_swz(x);
+        rowoff[r] = off;
+    }
+    const int j = tid % C, rg = tid / C;
+    uint32_t cx = 0;
+    uint64_t coff = 0;
+    for (int b = 0; b < K - M; b++)
+        if ((j >> b) & 1) {
+            cx |= 1u << p.col_local[b];
+            coff |= uint64_t(1) << p.tile_phys[p.col_local[b]];
+        }
+    const uint32_t cslot = tile_swz(cx);
+    float2 acc[RPT];
+#pragma unroll
+    for (int i = 0; i < RPT; i++) acc[i] = make_float2(0.f, 0.f);
+    for (int c = 0; c < R / KC; c++) {
+        if (c + 1 < R / KC) stage_slice(c + 1);
+        cp_async_commit();
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncthreads();
+        const float4* U4 = reinterpret_cast<const float4*>(Ubuf + (c & 1) * (KC * R));
+#pragma unroll 2
+        for (int kk = 0; kk < KC; kk++) {
+            const float2 b = tile[rowslot[c * KC + kk] ^ cslot];
+#pragma unroll
+            for (int i = 0; i < RPT; i += 2) {
+                const float4 u = U4[(kk * R + rg * RPT + i) >> 1];  // U(r,k), U(r+1,k)
+                acc[i].x += u.x * b.x - u.y * b.y;
+                acc[i].y += u.x * b.y + u.y * b.x;
+                acc[i + 1].x += u.z * b.x - u.w * b.y;
+                acc[i + 1].y += u.z * b.y + u.w * b.x;
+            }
+        }
+        __syncthreads();  // slice buffer c & 1 is refilled next iteration
+    }
+#pragma unroll
+    for (int i = 0; i < RPT; i++) state[base + rowoff[rg * RPT + i] + coff] = acc[i];
+}
+
+void launch_simt8(const TransmmLaunch& p, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        HQ_CHECK_CUDA(cudaFuncSetAttribute(k_transmm_simt8, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)kSimt8Smem));
+        attr = true;
+    }
+    k_transmm_simt8<<<(unsigned)p.ntiles, kSimtThreads, kSimt8Smem, st>>>(p);
+    HQ_CHECK_CUDA(cudaGetLastError());
+}
+
 template <int M>
 void launch_simt_m(const TransmmLaunch& p, cudaStream_t st) {
     constexpr int R = 1 << M;
@@ -177,7 +273,8 @@ void launch_transmm_simt(const TransmmLaunch& p, cudaStream_t st) {
         case 5: launch_simt_m<5>(p, st); break;
         case 6: launch_simt_m<6>(p, st); break;
         case 7: launch_simt_m<7>(p, st); break;
-        default: fail(HQ_ERR_UNSUPPORTED, "FP32 SIMT TransMM supports 4..7 group qubits, got %d", p.m);
+        case 8: launch_simt8(p, st); break;
+        default: fail(HQ_ERR_UNSUPPORTED, "FP32 SIMT TransMM supports 4..8 group qubits, got %d", p.m);
     }
 }
 
@@ -185,7 +282,7 @@ void launch_transmm_simt(const TransmmLaunch& p, cudaStream_t st) {
 
 // group widths each contraction runs (narrower groups are padded with idle qubits)
 static int min_mm_qubits(int precision) { return precision == HQ_MM_FP32 ? 4 : 6; }
-static int max_mm_qubits(int) { return 7; }
+static int max_mm_qubits(int) { return 8; }
 
 // Rows = the group's qubits padded up to the kernel's minimum with the lowest
 // free physical qubits; tile = rows + lowest non-row qubits up to 13 bits.
@@ -272,9 +369,10 @@ static TransmmLaunch make_launch(int n, int m, uint64_t rows, uint64_t tile, int
         p.piece_slot[mm] = tile_swz(local);
     }
     // sub-tiles for the tensor-core kernels: m = 6 (7 column bits) fixes the top
-    // column bit (64 x 64 sub-tiles), m = 7 (6 column bits) the top two (128 x 16)
-    if (m == 6 || m == 7) {
-        const int ncol = kSimtK - m, nsplit = m == 6 ? 1 : 2;
+    // column bit (64 x 64 sub-tiles), m = 7 (6 column bits) the top two (128 x 16),
+    // m = 8 (5 column bits) the top one (256 x 16)
+    if (m >= 6 && m <= 8) {
+        const int ncol = kSimtK - m, nsplit = m == 7 ? 2 : 1;
         const int sub_bits = kSimtK - nsplit;
         int sub[16];
         for (int j = 0; j < kSimtK; j++) sub[j] = 0;

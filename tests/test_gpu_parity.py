@@ -195,13 +195,29 @@ MM_TOL = {"fp32": (TOL, FID), "bf16x3": (TOL, FID), "tf32": (5e-5, 1e-5)}
 
 @pytest.mark.parametrize("prec,m", [("fp32", 4), ("fp32", 5), ("fp32", 6), ("fp32", 7),
                                     ("bf16x3", 4), ("bf16x3", 6), ("tf32", 6), ("bf16x3", 7),
-                                    ("tf32", 7)])
+                                    ("tf32", 7), ("fp32", 8), ("bf16x3", 8), ("tf32", 8)])
 def test_transmm_single_group(hq, oracle, prec, m):
     n = 17
     rng = W.SplitMix64(900 + m)
     qubits = sorted(rng.shuffle(range(n))[:m])
     desc = random_circuit(910 + m, n, 30 * m, qubits=qubits)
     psi = W.random_state(17, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    s.apply_transmm_group(W.to_gates(desc), sum(1 << q for q in qubits), prec)
+    tol, fid = MM_TOL[prec]
+    c = oracle.compare(oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+    assert c["max_abs_err"] <= tol and c["one_minus_fidelity"] <= fid, c
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32", "fp32"])
+def test_transmm_8_qubit_group_many_subtiles(hq, oracle, prec):
+    """An 8-qubit group on 22 qubits: 1024 sub-tiles over at most one CTA per SM,
+    so every CTA runs several sub-tiles and its operand ring wraps."""
+    n = 22
+    qubits = [0, 3, 5, 9, 12, 16, 19, 21]
+    desc = random_circuit(960, n, 200, qubits=qubits)
+    psi = W.random_state(23, n)
     s = hq.State(n, zero=False)
     s.load(psi)
     s.apply_transmm_group(W.to_gates(desc), sum(1 << q for q in qubits), prec)
@@ -225,7 +241,8 @@ def test_apply_caller_unitary_narrow_group(hq, oracle, prec):
 
 
 @pytest.mark.parametrize("prec,k", [("bf16x3", 6), ("tf32", 6), ("fp32", 6), ("bf16x3", 7),
-                                    ("tf32", 7), ("fp32", 7)])
+                                    ("tf32", 7), ("fp32", 7), ("bf16x3", 8), ("tf32", 8),
+                                    ("fp32", 8)])
 def test_transmm_qft_precision_sweep(hq, oracle, prec, k):
     """The QFT precision sweep at a size the oracle finishes: QFT on a random state,
     TransMM groups of k qubits only, per arithmetic."""
