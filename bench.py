@@ -435,6 +435,8 @@ def run_qft28(args, dist: Dist):
     for k in (6, 7, 8):
         for prec in ("bf16x3", "tf32", "fp32"):
             cases.append(("transmm", k, prec))
+    if args.qft_cases:  # e.g. "transmm:8:bf16x3,oshm:0:fp32"
+        cases = [(b, int(k), p) for b, k, p in (x.split(":") for x in args.qft_cases.split(","))]
     best = None
     for backend, k, prec in cases:
         rec = {"backend": backend, "k": k, "precision": prec}
@@ -457,7 +459,7 @@ def run_qft28(args, dist: Dist):
             rec.update({"ms": float(np.mean(ts)) / 1000.0, "passes": len(c.schedule()),
                         "max_abs_err": float(np.max(np.abs(g - ref))),
                         "one_minus_fidelity": float(1 - abs(ov) ** 2 / (refn * np.vdot(g, g).real))})
-            if backend == "transmm" and prec == "bf16x3" and k == 6:
+            if best is None or (backend == "transmm" and prec == "bf16x3" and k == 6):
                 best = rec
         except hq.HQError as e:
             rec["not_built"] = str(e)
@@ -467,7 +469,9 @@ def run_qft28(args, dist: Dist):
     value = best["ms"] if best else None
     peak, peak_kind = measured_peaks()
     achieved = (best["passes"] * 16.0 * N / (best["ms"] * 1e-3) / 1e9) if best else None
-    line = base_line(args, dist, f"{n}q QFT time (ms), TransMM split-BF16 k=6", value, "ms", value,
+    title = (f"TransMM {best['precision']} k={best['k']}" if best and best["backend"] == "transmm"
+             else "OShareMem")
+    line = base_line(args, dist, f"{n}q QFT time (ms), {title}", value, "ms", value,
                      False, f"QFT-{n} (H + CU1 for all pairs + swaps folded into the layout) on an "
                      "iid complex Gaussian normalised state; reference = exact transform (FP64 FFT)",
                      {"sweep": sweep})
@@ -684,6 +688,8 @@ def main():
     ap.add_argument("--workload", default="grid30",
                     choices=["grid30", "plain20", "qft28", "batch", "serve"])
     ap.add_argument("--qft-qubits", type=int, default=28)
+    ap.add_argument("--qft-cases", default="",
+                    help="backend:k:precision list for --workload qft28 (default: the full sweep)")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--serve-count", type=int, default=200)
     ap.add_argument("--serve-nmax", type=int, default=32)

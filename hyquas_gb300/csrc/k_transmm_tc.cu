@@ -364,270 +364,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc(const TransmmLaunc
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));
 }
 
-// ---- 7-qubit groups ---------------------------------------------------------
-// U (128 x 128 complex) no longer fits shared memory in real form, so the
-// product is taken in complex form over four real GEMMs into two accumulators:
-//     Cr = Ur.Br + Ui.(-Bi),   Ci = Ui.Br + Ur.Bi      (M = 128, N = 16, K = 128)
-// A holds Ur and Ui (split BF16 hi + lo, or TF32; 128 KB); each sub-tile of
-// 128 rows x 16 columns stages Br, Bi and -Bi.  The pipeline is the one of the
-// 6-qubit kernel (three staging buffers, two B buffers, two accumulator pairs).
-constexpr int T7_ROWS = 128;
-constexpr int T7_NSUB = 16;
-constexpr uint32_t SUB7_BYTES = 16384;   // a sub-tile, float2[2048]
-constexpr uint32_t SM7_A = 0;            // Ur, Ui: 128 KB
-constexpr uint32_t SM7_UI = 65536;
-constexpr uint32_t SM7_B = 131072;       // two buffers of 24 KB: Br | Bi | -Bi
-constexpr uint32_t B7_BYTES = 24576;
-constexpr uint32_t SM7_R = 180224;       // three staging buffers of 16 KB
-constexpr uint32_t SM7_MISC = 229376;
-constexpr uint32_t SM7_TOTAL = SM7_MISC + 1024;
-constexpr uint32_t TMEM7_COLS = 64;      // two buffers x (Cr 16 + Ci 16 columns)
-static_assert(SM7_TOTAL <= 232448, "shared memory per block");
-
-template <int PREC>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_transmm_tc7(const TransmmLaunch p) {
-    extern __shared__ __align__(1024) unsigned char smem[];
-    uint32_t* rowslot = reinterpret_cast<uint32_t*>(smem + SM7_MISC + 64);
-    uint32_t* colslot = rowslot + T7_ROWS;
-    const uint32_t sb = smem_u32(smem);
-    const uint32_t s_mbar = sb + SM7_MISC;
-    const uint32_t s_tslot = sb + SM7_MISC + 16;
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    float2* __restrict__ state = reinterpret_cast<float2*>(p.state);
-
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_tslot),
-                     "r"(TMEM7_COLS));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
-    }
-    if (t == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar + 8));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_mbar + 24));
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    __syncthreads();
-    if (t == 0) bulk_load(sb + SM7_A, p.umat, 131072u, s_mbar + 24);  // Ur, Ui: 128 KB
-    for (int r = t; r < T7_ROWS; r += TC_THREADS) {
-        uint32_t x = 0;
-        for (int b = 0; b < 7; b++)
-            if ((r >> b) & 1) x |= 1u << p.row_sub[b];
-        rowslot[r] = tile_swz(x);
-    }
-    for (int c = t; c < T7_NSUB; c += TC_THREADS) {
-        uint32_t x = 0;
-        for (int b = 0; b < 4; b++)
-            if ((c >> b) & 1) x |= 1u << p.col_sub[b];
-        colslot[c] = tile_swz(x);
-    }
-    const bool a_ok = mbar_wait(s_mbar + 24, 0);
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    const bool a_failed = __syncthreads_or(!a_ok);
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (a_failed && t == 0 && p.err) {
-        atomicCAS(p.err, 0, 1);
-        p.err[1] = 9;  // site: TransMM operand load
-    }
-    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + SM7_MISC + 16);
-
-    const uint64_t toff = local_to_phys(uint32_t(t) << 1, TC_TILE_BITS - 2, p.sub_phys);
-    const uint32_t tsl = tile_swz(uint32_t(t) << 1);
-    constexpr uint32_t esize = PREC == HQ_MM_TF32 ? 4 : 2;
-    constexpr uint32_t kstep_bytes = 256;
-    constexpr uint32_t sbo = (128 / (16 / esize)) * 128;
-    constexpr uint32_t a_lo = 32768;          // Ur / Ui lo halves (BF16x3)
-    constexpr uint32_t b_lo = 4096;           // Br / Bi / -Bi lo halves (BF16x3)
-    constexpr uint32_t idesc = make_idesc(PREC == HQ_MM_TF32 ? 2u : 1u, 128, T7_NSUB);
-    constexpr int nsteps = PREC == HQ_MM_TF32 ? 16 : 8;
-
-    const uint64_t nsub = p.ntiles * 4;
-    const uint64_t G = gridDim.x;
-    const uint64_t J = blockIdx.x < nsub ? (nsub - blockIdx.x + G - 1) / G : 0;
-    auto sub_base = [&](uint64_t j) {
-        const uint64_t v = blockIdx.x + j * G;
-        return tile_base(v >> 2, p.nruns, p.run_src, p.run_dst, p.run_len) +
-               (v & 1) * p.split_off[0] + ((v >> 1) & 1) * p.split_off[1];
-    };
-    auto load = [&](uint64_t j) {
-        if (j < J) {
-            const float2* gsrc = state + sub_base(j) + toff;
-            const uint32_t rb = sb + SM7_R + uint32_t(j % 3) * SUB7_BYTES;
-#pragma unroll
-            for (int m = 0; m < 4; m++)
-                cp_async16(rb + (tsl ^ p.sub_piece_slot[m]) * 8u, gsrc + p.sub_piece_off[m]);
-        }
-        cp_async_commit();
-    };
-    bool failed = a_failed;
-    // results of sub-tile j: (Cr, Ci) in TMEM columns 32 (j&1) and + 16 -> staging -> HBM
-    auto epilogue = [&](uint64_t j) {
-        const uint32_t b = uint32_t(j & 1);
-        const bool ok = mbar_wait(s_mbar + 8 * b, uint32_t((j >> 1) & 1));
-        if (__syncthreads_or(!ok)) {
-            if (t == 0 && p.err) {
-                atomicCAS(p.err, 0, 1);
-                p.err[1] = 7;  // site: TransMM accumulator wait
-                p.err[2] = (int)(j & 0x7fffffff);
-            }
-            failed = true;
-            return;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        float2* Rj = reinterpret_cast<float2*>(smem + SM7_R + uint32_t(j % 3) * SUB7_BYTES);
-        {
-            const int q = warp & 3, half = warp >> 2;
-            const int i = 32 * q + lane;  // D row = TMEM lane = row of the group
-            const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + 32 * b + 8 * half;
-            uint32_t vr[8], vi[8];
-            tmem_ld8(col, vr);
-            tmem_ld8(col + 16, vi);
-            const uint32_t rs = rowslot[i];
-#pragma unroll
-            for (int c = 0; c < 8; c++)
-                Rj[rs ^ colslot[8 * half + c]] = make_float2(__uint_as_float(vr[c]), __uint_as_float(vi[c]));
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
-        float2* gdst = state + sub_base(j) + toff;
-        const float4* R4 = reinterpret_cast<const float4*>(Rj);
-#pragma unroll
-        for (int m = 0; m < 4; m++)
-            *reinterpret_cast<float4*>(gdst + p.sub_piece_off[m]) = R4[(tsl ^ p.sub_piece_slot[m]) >> 1];
-        __syncthreads();
-    };
-
-    if (!failed) {
-        load(0);
-        load(1);
-    }
-    for (uint64_t j = 0; j < J && !failed; j++) {
-        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        __syncthreads();
-        // B blocks of sub-tile j: row n of each = column n; K = the group's row
-        {
-            const float2* Rj = reinterpret_cast<const float2*>(smem + SM7_R + uint32_t(j % 3) * SUB7_BYTES);
-            unsigned char* B = smem + SM7_B + uint32_t(j & 1) * B7_BYTES;
-            const int n = t & 15, rb = t >> 4;
-            const uint32_t cs = colslot[n];
-            float re[8], im[8];
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const float2 a = Rj[rowslot[rb * 8 + q] ^ cs];
-                re[q] = a.x;
-                im[q] = a.y;
-            }
-            if (PREC == HQ_MM_TF32) {
-#pragma unroll
-                for (int half = 0; half < 2; half++) {
-                    const uint32_t o = kmajor_off(n, rb * 8 + half * 4, 128, 4);
-                    const float4 vr = make_float4(to_tf32(re[4 * half]), to_tf32(re[4 * half + 1]),
-                                                  to_tf32(re[4 * half + 2]), to_tf32(re[4 * half + 3]));
-                    const float4 vi = make_float4(to_tf32(im[4 * half]), to_tf32(im[4 * half + 1]),
-                                                  to_tf32(im[4 * half + 2]), to_tf32(im[4 * half + 3]));
-                    *reinterpret_cast<float4*>(B + o) = vr;
-                    *reinterpret_cast<float4*>(B + 8192 + o) = vi;
-                    *reinterpret_cast<float4*>(B + 16384 + o) = make_float4(-vi.x, -vi.y, -vi.z, -vi.w);
-                }
-            } else {
-                uint32_t hre[4], lre[4], him[4], lim[4];
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const __nv_bfloat16 h0 = __float2bfloat16_rn(re[2 * q]);
-                    const __nv_bfloat16 h1 = __float2bfloat16_rn(re[2 * q + 1]);
-                    const __nv_bfloat16 l0 = __float2bfloat16_rn(re[2 * q] - __bfloat162float(h0));
-                    const __nv_bfloat16 l1 = __float2bfloat16_rn(re[2 * q + 1] - __bfloat162float(h1));
-                    hre[q] = pack_bf16(h0, h1);
-                    lre[q] = pack_bf16(l0, l1);
-                    const __nv_bfloat16 g0 = __float2bfloat16_rn(im[2 * q]);
-                    const __nv_bfloat16 g1 = __float2bfloat16_rn(im[2 * q + 1]);
-                    const __nv_bfloat16 k0 = __float2bfloat16_rn(im[2 * q] - __bfloat162float(g0));
-                    const __nv_bfloat16 k1 = __float2bfloat16_rn(im[2 * q + 1] - __bfloat162float(g1));
-                    him[q] = pack_bf16(g0, g1);
-                    lim[q] = pack_bf16(k0, k1);
-                }
-                const uint32_t o = kmajor_off(n, rb * 8, 128, 2);
-                const uint32_t sg = 0x80008000u;  // BF16 sign bits: -Bi exactly
-                *reinterpret_cast<uint4*>(B + o) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
-                *reinterpret_cast<uint4*>(B + b_lo + o) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
-                *reinterpret_cast<uint4*>(B + 8192 + o) = make_uint4(him[0], him[1], him[2], him[3]);
-                *reinterpret_cast<uint4*>(B + 8192 + b_lo + o) = make_uint4(lim[0], lim[1], lim[2], lim[3]);
-                *reinterpret_cast<uint4*>(B + 16384 + o) =
-                    make_uint4(him[0] ^ sg, him[1] ^ sg, him[2] ^ sg, him[3] ^ sg);
-                *reinterpret_cast<uint4*>(B + 16384 + b_lo + o) =
-                    make_uint4(lim[0] ^ sg, lim[1] ^ sg, lim[2] ^ sg, lim[3] ^ sg);
-            }
-        }
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
-
-        if (t == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t dr = tmem + 32 * uint32_t(j & 1), di = dr + 16;
-            const uint32_t bb = sb + SM7_B + uint32_t(j & 1) * B7_BYTES;
-            const uint32_t ur = sb + SM7_A, ui = sb + SM7_UI;
-            const uint32_t br = bb, bi = bb + 8192, bn = bb + 16384;
-            // D += A . B over K = 128; first = the accumulator starts at zero
-            auto gemm = [&](uint32_t d, uint32_t a, uint32_t bm, bool first) {
-                if (PREC == HQ_MM_TF32) {
-                    for (int kk = 0; kk < nsteps; kk++)
-                        mma_tf32(d, make_desc(a + kk * kstep_bytes, 128, sbo),
-                                 make_desc(bm + kk * kstep_bytes, 128, sbo), idesc, !first || kk > 0);
-                } else {
-                    for (int kk = 0; kk < nsteps; kk++)  // hi . hi
-                        mma_f16(d, make_desc(a + kk * kstep_bytes, 128, sbo),
-                                make_desc(bm + kk * kstep_bytes, 128, sbo), idesc, !first || kk > 0);
-                    for (int kk = 0; kk < nsteps; kk++)  // hi . lo
-                        mma_f16(d, make_desc(a + kk * kstep_bytes, 128, sbo),
-                                make_desc(bm + b_lo + kk * kstep_bytes, 128, sbo), idesc, 1);
-                    for (int kk = 0; kk < nsteps; kk++)  // lo . hi
-                        mma_f16(d, make_desc(a + a_lo + kk * kstep_bytes, 128, sbo),
-                                make_desc(bm + kk * kstep_bytes, 128, sbo), idesc, 1);
-                }
-            };
-            gemm(dr, ur, br, true);
-            gemm(dr, ui, bn, false);
-            gemm(di, ui, br, true);
-            gemm(di, ur, bi, false);
-            asm volatile(
-                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                    s_mbar + 8 * uint32_t(j & 1))
-                : "memory");
-        }
-        if (j > 0) epilogue(j - 1);
-        if (failed) break;
-        load(j + 2);
-    }
-    if (!failed && J > 0) epilogue(J - 1);
-    cp_async_wait_all();
-    if (a_failed) mbar_wait(s_mbar + 24, 0);  // the operand copies still in flight, bounded
-    __syncthreads();
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM7_COLS));
-}
-
-// A operand of a 7-qubit group from U (128 x 128, column-major complex128):
-// Ur and Ui, each 128 x 128 K-major (split BF16 hi at +0 and lo at +32 KB
-// of its 64 KB half, or TF32).
-__global__ void k_u_to_tc7(const double2* __restrict__ U, unsigned char* __restrict__ out, int prec) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= 128 * 128) return;
-    const int r = idx / 128, k = idx % 128;
-    const double2 u = U[(size_t)k * 128 + r];
-    const double v[2] = {u.x, u.y};
-    for (int part = 0; part < 2; part++) {
-        unsigned char* base = out + part * 65536;
-        if (prec == HQ_MM_TF32) {
-            *reinterpret_cast<float*>(base + kmajor_off(r, k, 128, 4)) = to_tf32((float)v[part]);
-        } else {
-            const __nv_bfloat16 hi = __float2bfloat16_rn((float)v[part]);
-            const __nv_bfloat16 lo = __float2bfloat16_rn((float)(v[part] - (double)__bfloat162float(hi)));
-            *reinterpret_cast<__nv_bfloat16*>(base + kmajor_off(r, k, 128, 2)) = hi;
-            *reinterpret_cast<__nv_bfloat16*>(base + 32768 + kmajor_off(r, k, 128, 2)) = lo;
-        }
-    }
-}
-
 // A operand from the FP64 unitary U (64 x 64, column-major): the real form
 // [[Ur, -Ui], [Ui, Ur]] (128 x 128) in the K-major core layout.
 __global__ void k_u_to_tc(const double2* __restrict__ U, unsigned char* __restrict__ out, int prec) {
@@ -651,36 +387,53 @@ __global__ void k_u_to_tc(const double2* __restrict__ U, unsigned char* __restri
     }
 }
 
-
-// ---- 8-qubit groups ---------------------------------------------------------
-// U (256 x 256 complex) as split BF16 or TF32 is 512 KB, more than shared
-// memory: it streams from L2 (every CTA reads the same 512 KB) through a ring
-// of three 32 KB chunks, each the Ur or Ui block of one 128-row half m of the
-// output over a 64-wide K slice s.  A sub-tile is 256 rows x 16 columns
-// (32 KB, the tile's top column bit fixed); per half m the complex product
-// runs as four real GEMMs (M = 128, N = 16, K = 256 in four slices):
-//     Cr(m) = Ur(m,:).Br + Ui(m,:).(-Bi),   Ci(m) = Ui(m,:).Br + Ur(m,:).Bi
-// Warp-specialised: warps 0-7 stage sub-tiles (cp.async), build B = Br | Bi |
-// -Bi and run the epilogue; warp 8 (one thread) streams the A chunks with bulk
-// copies and issues the MMAs.  Handshakes: bfull (B of sub-tile j written,
-// 256 arrivals), acc[j&1] (MMAs of j complete, tcgen05.commit), afull/aempty
-// per ring slot (bulk-copy bytes landed / the MMAs reading the slot complete).
-constexpr int T8_ROWS = 256;
-constexpr int T8_NSUB = 16;
-constexpr int T8_WORKERS = 256;
-constexpr int T8_THREADS = T8_WORKERS + 32;
-constexpr uint32_t SUB8_BYTES = 32768;  // a sub-tile, float2[4096]
-constexpr uint32_t SM8_R = 0;           // two staging buffers of 32 KB
-constexpr uint32_t SM8_B = 65536;       // Br | Bi | -Bi
-constexpr uint32_t B8_COMP = 16384;
-constexpr uint32_t SM8_A = SM8_B + 3 * B8_COMP;  // ring of A chunks
-constexpr uint32_t A8_CHUNK = 32768;
-constexpr int A8_SLOTS = 3;
-constexpr int A8_CHUNKS = 16;  // per sub-tile, chunk c = (m * 4 + s) * 2 + (0: Ur, 1: Ui)
-constexpr uint32_t SM8_MISC = SM8_A + A8_SLOTS * A8_CHUNK;
-constexpr uint32_t SM8_TOTAL = SM8_MISC + 2048;
-constexpr uint32_t TMEM8_COLS = 128;  // two buffers x (Cr0, Ci0, Cr1, Ci1) x 16 columns
-static_assert(SM8_TOTAL <= 232448, "shared memory per block");
+// ---- 7- and 8-qubit groups: U streamed, whole tiles -------------------------
+// U (2^KQ x 2^KQ complex) as split BF16 or TF32 is 128 KB (KQ = 7) or 512 KB
+// (KQ = 8).  It streams from L2 (every CTA reads the same bytes) through a
+// ring of three 32 KB chunks, each the Ur or Ui block of one 128-row half m of
+// the output over a 64-wide K slice s, chunk (m * KS + s) * 2 + part.  One
+// pass of the ring covers a whole 2^13-amplitude tile: ROWS = 2^KQ rows (the
+// group's qubits) x NCOL = 2^(13-KQ) columns, so every MMA has N = NCOL
+// (64 or 32; the tensor pipe's cost per MMA barely depends on N).  Per half m
+// the complex product runs as four real GEMMs (M = 128, N = NCOL, K = ROWS in
+// 64-wide slices) into three accumulators, the real part's two terms kept
+// apart and subtracted in the epilogue:
+//     P(m) = Ur(m,:).Br,  Q(m) = Ui(m,:).Bi,  Ci(m) = Ui(m,:).Br + Ur(m,:).Bi,
+//     Cr(m) = P(m) - Q(m)
+// Warp-specialised: warps 0-7 stage tiles (cp.async), build B = Br | Bi and
+// run the epilogue; warp 8 (one thread) streams the A chunks with bulk copies
+// and issues the MMAs.  Handshakes: bfull (B of tile j written, 256
+// arrivals), acc[j&1] (MMAs of tile j complete, tcgen05.commit), afull /
+// aempty per ring slot (bulk-copy bytes landed / the MMAs reading the slot
+// complete).  Tile j + 1 is staged while the MMAs of tile j run; its B is
+// built once they complete (one B buffer), while the accumulators are double
+// buffered so the epilogue of tile j - 1 overlaps the MMAs of tile j.
+template <int KQ>
+struct TcsShape {
+    static constexpr int ROWS = 1 << KQ;
+    static constexpr int NCOL = (1 << 13) / ROWS;
+    static constexpr int MB = ROWS / 128;        // 128-row output halves
+    static constexpr int KS = ROWS / 64;         // 64-wide K slices
+    static constexpr int CHUNKS = MB * KS * 2;   // A chunks per tile
+    static constexpr int RPT = ROWS * NCOL / 256;  // B rows a worker converts
+    static_assert(MB * 3 * NCOL <= 256, "accumulators of one buffer");
+};
+constexpr int TS_WORKERS = 256;
+constexpr int TS_THREADS = TS_WORKERS + 32;
+constexpr uint32_t SMS_R = 0;                         // the tile, float2[8192]
+constexpr uint32_t SMS_B = 65536;                     // Br | Bi
+constexpr uint32_t BS_COMP = 32768;
+constexpr uint32_t SMS_A = SMS_B + 2 * BS_COMP;       // ring of A chunks
+constexpr uint32_t AS_CHUNK = 32768;
+constexpr int AS_SLOTS = 3;
+constexpr uint32_t SMS_MISC = SMS_A + AS_SLOTS * AS_CHUNK;
+constexpr uint32_t SMS_TOTAL = SMS_MISC + 2048;
+static_assert(SMS_TOTAL <= 232448, "shared memory per block");
+// MISC: mbarriers and the TMEM slot, piece tables at + 128, slot tables at + 512
+constexpr uint32_t MBS_ACC = 8, MBS_AFULL = 24, MBS_AEMPTY = MBS_AFULL + 8 * AS_SLOTS,
+                   MBS_FIN = MBS_AEMPTY + 8 * AS_SLOTS, MBS_TSLOT = MBS_FIN + 8;
+static_assert(MBS_TSLOT + 4 <= 128, "MISC head");
+constexpr uint32_t TMEMS_COLS = 512;  // accumulator buffer b at column 256 b
 
 // bar.sync / bar.red over the 256 worker threads only (barrier 1)
 __device__ __forceinline__ void workers_sync() { asm volatile("bar.sync 1, 256;\n" ::: "memory"); }
@@ -703,64 +456,71 @@ __device__ __forceinline__ void set_err(int* err, int site, uint64_t detail) {
     }
 }
 
-template <int PREC>
-__global__ void __launch_bounds__(T8_THREADS, 1) k_transmm_tc8(const TransmmLaunch p) {
+template <int KQ, int PREC>
+__global__ void __launch_bounds__(TS_THREADS, 1) k_transmm_tcs(const TransmmLaunch p) {
+    using S = TcsShape<KQ>;
     extern __shared__ __align__(1024) unsigned char smem[];
-    uint32_t* rowslot = reinterpret_cast<uint32_t*>(smem + SM8_MISC + 256);
-    uint32_t* colslot = rowslot + T8_ROWS;
+    uint64_t* poff = reinterpret_cast<uint64_t*>(smem + SMS_MISC + 128);     // 16 pieces
+    uint32_t* pslot = reinterpret_cast<uint32_t*>(smem + SMS_MISC + 256);    // 16 pieces
+    uint32_t* rowslot = reinterpret_cast<uint32_t*>(smem + SMS_MISC + 512);  // up to 256
+    uint32_t* colslot = rowslot + S::ROWS;                                   // up to 64
     const uint32_t sb = smem_u32(smem);
-    const uint32_t m_bfull = sb + SM8_MISC, m_acc = m_bfull + 8, m_afull = m_bfull + 24,
-                   m_aempty = m_bfull + 48, m_fin = m_bfull + 72, s_tslot = m_bfull + 80;
+    const uint32_t m_bfull = sb + SMS_MISC, m_acc = m_bfull + MBS_ACC, m_afull = m_bfull + MBS_AFULL,
+                   m_aempty = m_bfull + MBS_AEMPTY, m_fin = m_bfull + MBS_FIN, s_tslot = m_bfull + MBS_TSLOT;
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     float2* __restrict__ state = reinterpret_cast<float2*>(p.state);
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_tslot),
-                     "r"(TMEM8_COLS));
+                     "r"(TMEMS_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (t == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(m_bfull), "r"(T8_WORKERS));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(m_bfull), "r"(TS_WORKERS));
         for (int i = 0; i < 2; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(m_acc + 8 * i));
-        for (int i = 0; i < A8_SLOTS; i++) {
+        for (int i = 0; i < AS_SLOTS; i++) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(m_afull + 8 * i));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(m_aempty + 8 * i));
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(m_fin));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    for (int r = t; r < T8_ROWS; r += T8_THREADS) {
+    if (t < 16) {  // piece mm of a thread = tile local index 2 t + 512 mm
+        poff[t] = local_to_phys(uint32_t(t) << 9, TC_TILE_BITS, p.tile_phys);
+        pslot[t] = tile_swz(uint32_t(t) << 9);
+    }
+    for (int r = t; r < S::ROWS; r += TS_THREADS) {
         uint32_t x = 0;
-        for (int b = 0; b < 8; b++)
-            if ((r >> b) & 1) x |= 1u << p.row_sub[b];
+        for (int b = 0; b < KQ; b++)
+            if ((r >> b) & 1) x |= 1u << p.row_local[b];
         rowslot[r] = tile_swz(x);
     }
-    for (int c = t; c < T8_NSUB; c += T8_THREADS) {
+    for (int c = t; c < S::NCOL; c += TS_THREADS) {
         uint32_t x = 0;
-        for (int b = 0; b < 4; b++)
-            if ((c >> b) & 1) x |= 1u << p.col_sub[b];
+        for (int b = 0; b < TC_TILE_BITS - KQ; b++)
+            if ((c >> b) & 1) x |= 1u << p.col_local[b];
         colslot[c] = tile_swz(x);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + SM8_MISC + 80);
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + SMS_MISC + MBS_TSLOT);
 
     constexpr uint32_t esize = PREC == HQ_MM_TF32 ? 4 : 2;
-    const uint64_t nsub = p.ntiles * 2;
+    constexpr uint32_t per_core = 16 / esize;
     const uint64_t G = gridDim.x;
-    const uint64_t J = blockIdx.x < nsub ? (nsub - blockIdx.x + G - 1) / G : 0;
+    const uint64_t J = blockIdx.x < p.ntiles ? (p.ntiles - blockIdx.x + G - 1) / G : 0;
 
-    if (warp == T8_WORKERS / 32) {
+    if (warp == TS_WORKERS / 32) {
         // ---- A stream + MMA issue (one thread) ----
         if (lane == 0 && J > 0) {
-            constexpr uint32_t sbo_a = (64 / (16 / esize)) * 128;   // A chunk: 128 rows x 64 K
-            constexpr uint32_t sbo_b = (256 / (16 / esize)) * 128;  // B: 16 rows x 256 K
-            constexpr uint32_t slice_b = (64 / (16 / esize)) * 128; // B offset of one K slice
-            constexpr uint32_t a_lo = 16384;                        // A chunk lo half (BF16x3)
-            constexpr uint32_t b_lo = 8192;                         // B component lo half
-            constexpr uint32_t idesc = make_idesc(PREC == HQ_MM_TF32 ? 2u : 1u, 128, T8_NSUB);
-            constexpr int nsteps = PREC == HQ_MM_TF32 ? 8 : 4;      // 32 bytes of K per MMA
+            constexpr uint32_t sbo_a = (64 / per_core) * 128;        // A chunk: 128 rows x 64 K
+            constexpr uint32_t sbo_b = (S::ROWS / per_core) * 128;   // B: NCOL rows x ROWS K
+            constexpr uint32_t slice_b = (64 / per_core) * 128;      // B offset of one K slice
+            constexpr uint32_t a_lo = 16384;                         // A chunk lo half (BF16x3)
+            constexpr uint32_t b_lo = S::NCOL * S::ROWS * 2;         // B component lo half (BF16x3)
+            constexpr uint32_t idesc = make_idesc(PREC == HQ_MM_TF32 ? 2u : 1u, 128, S::NCOL);
+            constexpr int nsteps = PREC == HQ_MM_TF32 ? 8 : 4;       // 32 bytes of K per MMA
             const char* umat = reinterpret_cast<const char*>(p.umat);
             auto gemm = [&](uint32_t d, uint32_t a, uint32_t bm, bool first) {
                 if (PREC == HQ_MM_TF32) {
@@ -779,54 +539,52 @@ __global__ void __launch_bounds__(T8_THREADS, 1) k_transmm_tc8(const TransmmLaun
                                 make_desc(bm + kk * 256, 128, sbo_b), idesc, 1);
                 }
             };
-            const uint64_t total = J * A8_CHUNKS;
+            const uint64_t total = J * S::CHUNKS;
             uint64_t issued = 0, consumed = 0;
             auto fetch = [&](uint64_t h) {
-                const uint32_t slot = uint32_t(h % A8_SLOTS);
-                bulk_load(sb + SM8_A + slot * A8_CHUNK, umat + (h % A8_CHUNKS) * A8_CHUNK, A8_CHUNK,
+                const uint32_t slot = uint32_t(h % AS_SLOTS);
+                bulk_load(sb + SMS_A + slot * AS_CHUNK, umat + (h % S::CHUNKS) * AS_CHUNK, AS_CHUNK,
                           m_afull + 8 * slot);
                 issued = h + 1;
             };
-            fetch(0);
-            if (total > 1) fetch(1);
+            for (uint64_t h = 0; h + 1 < AS_SLOTS && h < total; h++) fetch(h);
             bool ok = true;
             for (uint64_t j = 0; j < J && ok; j++) {
                 if (!mbar_wait(m_bfull, uint32_t(j & 1))) {
                     set_err(p.err, 10, j);  // site: TransMM operand B handshake
-                    ok = false;
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                const uint32_t accb = tmem + 64 * uint32_t(j & 1);
-                for (int c = 0; c < A8_CHUNKS; c++) {
-                    const uint64_t g = j * A8_CHUNKS + c;
-                    const uint32_t slot = uint32_t(g % A8_SLOTS);
-                    if (!mbar_wait(m_afull + 8 * slot, uint32_t((g / A8_SLOTS) & 1))) {
+                const uint32_t accb = tmem + 256 * uint32_t(j & 1);
+                for (int c = 0; c < S::CHUNKS; c++) {
+                    const uint64_t g = j * S::CHUNKS + c;
+                    const uint32_t slot = uint32_t(g % AS_SLOTS);
+                    if (!mbar_wait(m_afull + 8 * slot, uint32_t((g / AS_SLOTS) & 1))) {
                         set_err(p.err, 9, g);  // site: TransMM operand load
                         ok = false;
                         break;
                     }
                     consumed = g + 1;
-                    const int m = c >> 3, s = (c >> 1) & 3, part = c & 1;
-                    const uint32_t a = sb + SM8_A + slot * A8_CHUNK;
-                    const uint32_t dr = accb + 32 * m, di = dr + 16;
-                    const uint32_t br = sb + SM8_B + s * slice_b, bi = br + B8_COMP, bn = br + 2 * B8_COMP;
+                    const int m = c / (2 * S::KS), s = (c >> 1) % S::KS, part = c & 1;
+                    const uint32_t a = sb + SMS_A + slot * AS_CHUNK;
+                    const uint32_t dp = accb + 3 * S::NCOL * m, dq = dp + S::NCOL, di = dp + 2 * S::NCOL;
+                    const uint32_t br = sb + SMS_B + s * slice_b, bi = br + BS_COMP;
                     if (part == 0) {
-                        gemm(dr, a, br, s == 0);
+                        gemm(dp, a, br, s == 0);
                         gemm(di, a, bi, s == 0);
                     } else {
-                        gemm(dr, a, bn, false);
+                        gemm(dq, a, bi, s == 0);
                         gemm(di, a, br, false);
                     }
                     asm volatile(
                         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                             m_aempty + 8 * slot)
                         : "memory");
-                    // refill: chunk g + 2 goes where chunk g - 1 was, once its MMAs completed
-                    const uint64_t h = g + 2;
+                    // refill: chunk g + SLOTS - 1 goes where chunk g - 1 was, once its MMAs completed
+                    const uint64_t h = g + AS_SLOTS - 1;
                     if (h < total) {
-                        if (h >= A8_SLOTS &&
-                            !mbar_wait(m_aempty + 8 * uint32_t(h % A8_SLOTS), uint32_t(((h - A8_SLOTS) / A8_SLOTS) & 1))) {
+                        if (h >= AS_SLOTS && !mbar_wait(m_aempty + 8 * uint32_t(h % AS_SLOTS),
+                                                        uint32_t(((h - AS_SLOTS) / AS_SLOTS) & 1))) {
                             set_err(p.err, 9, h);
                             ok = false;
                             break;
@@ -846,59 +604,61 @@ __global__ void __launch_bounds__(T8_THREADS, 1) k_transmm_tc8(const TransmmLaun
                          : "memory");
             mbar_wait(m_fin, 0);
             for (uint64_t h = consumed; h < issued; h++)
-                mbar_wait(m_afull + 8 * uint32_t(h % A8_SLOTS), uint32_t((h / A8_SLOTS) & 1));
+                mbar_wait(m_afull + 8 * uint32_t(h % AS_SLOTS), uint32_t((h / AS_SLOTS) & 1));
         }
         __syncwarp();
     } else {
         // ---- workers: staging, B, epilogue ----
-        const uint64_t toff = local_to_phys(uint32_t(t) << 1, TC_TILE_BITS - 1, p.sub_phys);
+        const uint64_t toff = local_to_phys(uint32_t(t) << 1, TC_TILE_BITS, p.tile_phys);
         const uint32_t tsl = tile_swz(uint32_t(t) << 1);
-        auto sub_base = [&](uint64_t j) {
-            const uint64_t v = blockIdx.x + j * G;
-            return tile_base(v >> 1, p.nruns, p.run_src, p.run_dst, p.run_len) + (v & 1) * p.split_off[0];
+        auto tbase = [&](uint64_t j) {
+            return tile_base(blockIdx.x + j * G, p.nruns, p.run_src, p.run_dst, p.run_len);
         };
         auto load = [&](uint64_t j) {
             if (j < J) {
-                const float2* gsrc = state + sub_base(j) + toff;
-                const uint32_t rb = sb + SM8_R + uint32_t(j & 1) * SUB8_BYTES;
+                const float2* gsrc = state + tbase(j) + toff;
 #pragma unroll
-                for (int m = 0; m < 8; m++)
-                    cp_async16(rb + (tsl ^ p.sub_piece_slot[m]) * 8u, gsrc + p.sub_piece_off[m]);
+                for (int mm = 0; mm < 16; mm++)
+                    cp_async16(sb + SMS_R + (tsl ^ pslot[mm]) * 8u, gsrc + poff[mm]);
             }
             cp_async_commit();
         };
-        // results of sub-tile j: TMEM buffer j&1 -> over its staging buffer -> HBM
+        float2* R = reinterpret_cast<float2*>(smem + SMS_R);
+        // results of tile j: TMEM buffer j&1 -> R -> HBM.  Warp (q, h): TMEM
+        // lanes 32 q .. 32 q + 31 of half m = h (KQ = 8) or of columns 32 h .. (KQ = 7)
         auto epilogue = [&](uint64_t j) {
             const uint32_t b = uint32_t(j & 1);
-            float2* Rj = reinterpret_cast<float2*>(smem + SM8_R + b * SUB8_BYTES);
-            const int q = warp & 3, m = warp >> 2;
-            const int i = 128 * m + 32 * q + lane;  // row of the group = TMEM lane 32 q + lane of half m
-            const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + 64 * b + 32 * m;
+            const int q = warp & 3, h = warp >> 2;
+            const int m = S::MB == 2 ? h : 0, c0 = S::MB == 2 ? 0 : 32 * h;
+            const int i = 128 * m + 32 * q + lane;  // row of the group
+            const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + 256 * b + 3 * S::NCOL * m + c0;
             const uint32_t rs = rowslot[i];
 #pragma unroll
-            for (int half = 0; half < 2; half++) {
-                uint32_t vr[8], vi[8];
-                tmem_ld8(col + 8 * half, vr);
-                tmem_ld8(col + 16 + 8 * half, vi);
+            for (int c8 = 0; c8 < 4; c8++) {
+                uint32_t vp[8], vq[8], vi[8];
+                tmem_ld8(col + 8 * c8, vp);
+                tmem_ld8(col + S::NCOL + 8 * c8, vq);
+                tmem_ld8(col + 2 * S::NCOL + 8 * c8, vi);
 #pragma unroll
                 for (int c = 0; c < 8; c++)
-                    Rj[rs ^ colslot[8 * half + c]] = make_float2(__uint_as_float(vr[c]), __uint_as_float(vi[c]));
+                    R[rs ^ colslot[c0 + 8 * c8 + c]] =
+                        make_float2(__uint_as_float(vp[c]) - __uint_as_float(vq[c]), __uint_as_float(vi[c]));
             }
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             workers_sync();
-            float2* gdst = state + sub_base(j) + toff;
-            const float4* R4 = reinterpret_cast<const float4*>(Rj);
+            float2* gdst = state + tbase(j) + toff;
+            const float4* R4 = reinterpret_cast<const float4*>(R);
 #pragma unroll
-            for (int mm = 0; mm < 8; mm++)
-                *reinterpret_cast<float4*>(gdst + p.sub_piece_off[mm]) = R4[(tsl ^ p.sub_piece_slot[mm]) >> 1];
+            for (int mm = 0; mm < 16; mm++)
+                *reinterpret_cast<float4*>(gdst + poff[mm]) = R4[(tsl ^ pslot[mm]) >> 1];
             workers_sync();
         };
         bool failed = false;
         load(0);
         for (uint64_t j = 0; j < J; j++) {
-            cp_async_wait_all();  // sub-tile j staged
+            cp_async_wait_all();  // tile j staged
             workers_sync();
-            if (j > 0) {  // MMAs of j - 1 complete: B is free, accumulators j - 1 ready
+            if (j > 0) {  // MMAs of tile j - 1 complete: B is free, accumulators j - 1 ready
                 const bool ok = mbar_wait(m_acc + 8 * uint32_t((j - 1) & 1), uint32_t(((j - 1) >> 1) & 1));
                 if (workers_any(!ok)) {
                     if (t == 0) set_err(p.err, 7, j - 1);  // site: TransMM accumulator wait
@@ -908,66 +668,56 @@ __global__ void __launch_bounds__(T8_THREADS, 1) k_transmm_tc8(const TransmmLaun
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             }
             {
-                const float2* Rj = reinterpret_cast<const float2*>(smem + SM8_R + uint32_t(j & 1) * SUB8_BYTES);
-                unsigned char* B = smem + SM8_B;
-                const int n = t & 15, rb = t >> 4;  // column n, rows 16 rb .. 16 rb + 15
+                unsigned char* B = smem + SMS_B;
+                const int n = t % S::NCOL, rb = t / S::NCOL;  // column n, rows RPT rb .. RPT rb + RPT - 1
                 const uint32_t cs = colslot[n];
-                float re[16], im[16];
-#pragma unroll
-                for (int qq = 0; qq < 16; qq++) {
-                    const float2 a = Rj[rowslot[rb * 16 + qq] ^ cs];
-                    re[qq] = a.x;
-                    im[qq] = a.y;
-                }
                 if (PREC == HQ_MM_TF32) {
 #pragma unroll
-                    for (int h4 = 0; h4 < 4; h4++) {
-                        const uint32_t o = kmajor_off(n, rb * 16 + 4 * h4, 256, 4);
-                        const float4 vr = make_float4(to_tf32(re[4 * h4]), to_tf32(re[4 * h4 + 1]),
-                                                      to_tf32(re[4 * h4 + 2]), to_tf32(re[4 * h4 + 3]));
-                        const float4 vi = make_float4(to_tf32(im[4 * h4]), to_tf32(im[4 * h4 + 1]),
-                                                      to_tf32(im[4 * h4 + 2]), to_tf32(im[4 * h4 + 3]));
-                        *reinterpret_cast<float4*>(B + o) = vr;
-                        *reinterpret_cast<float4*>(B + B8_COMP + o) = vi;
-                        *reinterpret_cast<float4*>(B + 2 * B8_COMP + o) = make_float4(-vi.x, -vi.y, -vi.z, -vi.w);
+                    for (int h4 = 0; h4 < S::RPT / 4; h4++) {
+                        float re[4], im[4];
+#pragma unroll
+                        for (int qq = 0; qq < 4; qq++) {
+                            const float2 a = R[rowslot[rb * S::RPT + 4 * h4 + qq] ^ cs];
+                            re[qq] = to_tf32(a.x);
+                            im[qq] = to_tf32(a.y);
+                        }
+                        const uint32_t o = kmajor_off(n, rb * S::RPT + 4 * h4, S::ROWS, 4);
+                        *reinterpret_cast<float4*>(B + o) = make_float4(re[0], re[1], re[2], re[3]);
+                        *reinterpret_cast<float4*>(B + BS_COMP + o) = make_float4(im[0], im[1], im[2], im[3]);
                     }
                 } else {
-                    constexpr uint32_t b_lo = 8192;
-                    const uint32_t sg = 0x80008000u;  // BF16 sign bits: -Bi exactly
+                    constexpr uint32_t b_lo = S::NCOL * S::ROWS * 2;
 #pragma unroll
-                    for (int h8 = 0; h8 < 2; h8++) {
+                    for (int h8 = 0; h8 < S::RPT / 8; h8++) {
                         uint32_t hre[4], lre[4], him[4], lim[4];
 #pragma unroll
                         for (int qq = 0; qq < 4; qq++) {
-                            const float x0 = re[8 * h8 + 2 * qq], x1 = re[8 * h8 + 2 * qq + 1];
-                            const float y0 = im[8 * h8 + 2 * qq], y1 = im[8 * h8 + 2 * qq + 1];
-                            const __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
-                            const __nv_bfloat16 g0 = __float2bfloat16_rn(y0), g1 = __float2bfloat16_rn(y1);
+                            const float2 a0 = R[rowslot[rb * S::RPT + 8 * h8 + 2 * qq] ^ cs];
+                            const float2 a1 = R[rowslot[rb * S::RPT + 8 * h8 + 2 * qq + 1] ^ cs];
+                            const __nv_bfloat16 h0 = __float2bfloat16_rn(a0.x), h1 = __float2bfloat16_rn(a1.x);
+                            const __nv_bfloat16 g0 = __float2bfloat16_rn(a0.y), g1 = __float2bfloat16_rn(a1.y);
                             hre[qq] = pack_bf16(h0, h1);
-                            lre[qq] = pack_bf16(__float2bfloat16_rn(x0 - __bfloat162float(h0)),
-                                                __float2bfloat16_rn(x1 - __bfloat162float(h1)));
+                            lre[qq] = pack_bf16(__float2bfloat16_rn(a0.x - __bfloat162float(h0)),
+                                                __float2bfloat16_rn(a1.x - __bfloat162float(h1)));
                             him[qq] = pack_bf16(g0, g1);
-                            lim[qq] = pack_bf16(__float2bfloat16_rn(y0 - __bfloat162float(g0)),
-                                                __float2bfloat16_rn(y1 - __bfloat162float(g1)));
+                            lim[qq] = pack_bf16(__float2bfloat16_rn(a0.y - __bfloat162float(g0)),
+                                                __float2bfloat16_rn(a1.y - __bfloat162float(g1)));
                         }
-                        const uint32_t o = kmajor_off(n, rb * 16 + 8 * h8, 256, 2);
+                        const uint32_t o = kmajor_off(n, rb * S::RPT + 8 * h8, S::ROWS, 2);
                         *reinterpret_cast<uint4*>(B + o) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
                         *reinterpret_cast<uint4*>(B + b_lo + o) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
-                        *reinterpret_cast<uint4*>(B + B8_COMP + o) = make_uint4(him[0], him[1], him[2], him[3]);
-                        *reinterpret_cast<uint4*>(B + B8_COMP + b_lo + o) =
+                        *reinterpret_cast<uint4*>(B + BS_COMP + o) = make_uint4(him[0], him[1], him[2], him[3]);
+                        *reinterpret_cast<uint4*>(B + BS_COMP + b_lo + o) =
                             make_uint4(lim[0], lim[1], lim[2], lim[3]);
-                        *reinterpret_cast<uint4*>(B + 2 * B8_COMP + o) =
-                            make_uint4(him[0] ^ sg, him[1] ^ sg, him[2] ^ sg, him[3] ^ sg);
-                        *reinterpret_cast<uint4*>(B + 2 * B8_COMP + b_lo + o) =
-                            make_uint4(lim[0] ^ sg, lim[1] ^ sg, lim[2] ^ sg, lim[3] ^ sg);
                     }
                 }
             }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(m_bfull) : "memory");
+            workers_sync();  // R is read: the epilogue may write over it
             if (j > 0) epilogue(j - 1);
-            load(j + 1);  // into the buffer sub-tile j - 1 just left
+            load(j + 1);
         }
         if (!failed && J > 0) {
             const bool ok = mbar_wait(m_acc + 8 * uint32_t((J - 1) & 1), uint32_t(((J - 1) >> 1) & 1));
@@ -983,22 +733,25 @@ __global__ void __launch_bounds__(T8_THREADS, 1) k_transmm_tc8(const TransmmLaun
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM8_COLS));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEMS_COLS));
 }
 
-// A operand of an 8-qubit group from U (256 x 256, column-major complex128):
-// 16 chunks of 32 KB in the order the kernel consumes them, chunk
-// (m * 4 + s) * 2 + part = Ur (part 0) or Ui (part 1) of rows 128 m .. 128 m + 127
-// and K 64 s .. 64 s + 63, K-major (split BF16 hi at +0 and lo at +16 KB, or TF32).
-__global__ void k_u_to_tc8(const double2* __restrict__ U, unsigned char* __restrict__ out, int prec) {
+// A operand of a 7- or 8-qubit group from U (2^KQ x 2^KQ, column-major
+// complex128): the chunks in the order the kernel consumes them, chunk
+// (m * KS + s) * 2 + part = Ur (part 0) or Ui (part 1) of output rows
+// 128 m .. 128 m + 127 and K 64 s .. 64 s + 63, K-major (split BF16 hi at +0
+// and lo at +16 KB, or TF32).
+template <int KQ>
+__global__ void k_u_to_tcs(const double2* __restrict__ U, unsigned char* __restrict__ out, int prec) {
+    using S = TcsShape<KQ>;
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= 256 * 256) return;
-    const int r = idx / 256, k = idx % 256;
-    const double2 u = U[(size_t)k * 256 + r];
+    if (idx >= S::ROWS * S::ROWS) return;
+    const int r = idx / S::ROWS, k = idx % S::ROWS;
+    const double2 u = U[(size_t)k * S::ROWS + r];
     const double v[2] = {u.x, u.y};
     const int m = r >> 7, rr = r & 127, s = k >> 6, kk = k & 63;
     for (int part = 0; part < 2; part++) {
-        unsigned char* base = out + size_t((m * 4 + s) * 2 + part) * A8_CHUNK;
+        unsigned char* base = out + size_t((m * S::KS + s) * 2 + part) * AS_CHUNK;
         if (prec == HQ_MM_TF32) {
             *reinterpret_cast<float*>(base + kmajor_off(rr, kk, 64, 4)) = to_tf32((float)v[part]);
         } else {
@@ -1016,7 +769,7 @@ size_t transmm_tc_operand_bytes(int m, int precision) {
     (void)precision;
     HQ_REQUIRE(m >= 6 && m <= 8, HQ_ERR_UNSUPPORTED,
                "tensor-core TransMM runs 6- to 8-qubit groups (got %d)", m);
-    return m == 6 ? 65536 : m == 7 ? 131072 : size_t(A8_CHUNKS) * A8_CHUNK;
+    return m == 6 ? 65536 : m == 7 ? size_t(TcsShape<7>::CHUNKS) * AS_CHUNK : size_t(TcsShape<8>::CHUNKS) * AS_CHUNK;
 }
 
 void launch_u_to_tc_operand(int m, int precision, const double* d_u, void* d_out, cudaStream_t st) {
@@ -1025,9 +778,9 @@ void launch_u_to_tc_operand(int m, int precision, const double* d_u, void* d_out
     if (m == 6)
         k_u_to_tc<<<64, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
     else if (m == 7)
-        k_u_to_tc7<<<64, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
+        k_u_to_tcs<7><<<64, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
     else
-        k_u_to_tc8<<<256, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
+        k_u_to_tcs<8><<<256, 256, 0, st>>>((const double2*)d_u, (unsigned char*)d_out, precision);
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -1045,48 +798,35 @@ static void launch_prec(const TransmmLaunch& p, cudaStream_t st) {
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 
-template <int PREC>
-static void launch_prec7(const TransmmLaunch& p, cudaStream_t st) {
+template <int KQ, int PREC>
+static void launch_streamed(const TransmmLaunch& p, cudaStream_t st) {
     static bool attr = false;
     if (!attr) {
-        HQ_CHECK_CUDA(cudaFuncSetAttribute(k_transmm_tc7<PREC>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM7_TOTAL));
+        HQ_CHECK_CUDA(cudaFuncSetAttribute(k_transmm_tcs<KQ, PREC>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMS_TOTAL));
         attr = true;
     }
     const uint64_t slots = uint64_t(ctx().sm_count);
-    const unsigned grid = (unsigned)(p.ntiles * 4 < slots ? p.ntiles * 4 : slots);
-    k_transmm_tc7<PREC><<<grid, TC_THREADS, SM7_TOTAL, st>>>(p);
-    HQ_CHECK_CUDA(cudaGetLastError());
-}
-
-template <int PREC>
-static void launch_prec8(const TransmmLaunch& p, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        HQ_CHECK_CUDA(cudaFuncSetAttribute(k_transmm_tc8<PREC>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM8_TOTAL));
-        attr = true;
-    }
-    const uint64_t slots = uint64_t(ctx().sm_count);
-    const unsigned grid = (unsigned)(p.ntiles * 2 < slots ? p.ntiles * 2 : slots);
-    k_transmm_tc8<PREC><<<grid, T8_THREADS, SM8_TOTAL, st>>>(p);
+    const unsigned grid = (unsigned)(p.ntiles < slots ? p.ntiles : slots);
+    k_transmm_tcs<KQ, PREC><<<grid, TS_THREADS, SMS_TOTAL, st>>>(p);
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 
 void launch_transmm_tc(const TransmmLaunch& p, cudaStream_t st) {
     HQ_REQUIRE(p.m >= 6 && p.m <= 8 && p.k == TC_TILE_BITS, HQ_ERR_UNSUPPORTED,
                "tensor-core TransMM runs 6- to 8-qubit groups on 13-qubit tiles");
+    const bool tf32 = p.precision == HQ_MM_TF32;
     if (p.m == 8) {
-        if (p.precision == HQ_MM_TF32)
-            launch_prec8<HQ_MM_TF32>(p, st);
+        if (tf32)
+            launch_streamed<8, HQ_MM_TF32>(p, st);
         else
-            launch_prec8<HQ_MM_BF16X3>(p, st);
+            launch_streamed<8, HQ_MM_BF16X3>(p, st);
     } else if (p.m == 7) {
-        if (p.precision == HQ_MM_TF32)
-            launch_prec7<HQ_MM_TF32>(p, st);
+        if (tf32)
+            launch_streamed<7, HQ_MM_TF32>(p, st);
         else
-            launch_prec7<HQ_MM_BF16X3>(p, st);
-    } else if (p.precision == HQ_MM_TF32) {
+            launch_streamed<7, HQ_MM_BF16X3>(p, st);
+    } else if (tf32) {
         launch_prec<HQ_MM_TF32>(p, st);
     } else {
         launch_prec<HQ_MM_BF16X3>(p, st);

@@ -368,11 +368,10 @@ static TransmmLaunch make_launch(int n, int m, uint64_t rows, uint64_t tile, int
         p.piece_off[mm] = off;
         p.piece_slot[mm] = tile_swz(local);
     }
-    // sub-tiles for the tensor-core kernels: m = 6 (7 column bits) fixes the top
-    // column bit (64 x 64 sub-tiles), m = 7 (6 column bits) the top two (128 x 16),
-    // m = 8 (5 column bits) the top one (256 x 16)
-    if (m >= 6 && m <= 8) {
-        const int ncol = kSimtK - m, nsplit = m == 7 ? 2 : 1;
+    // sub-tiles for the 6-qubit tensor-core kernel: the top column bit fixed
+    // (64 x 64 sub-tiles); the 7- and 8-qubit kernels take whole tiles
+    if (m == 6) {
+        const int ncol = kSimtK - m, nsplit = 1;
         const int sub_bits = kSimtK - nsplit;
         int sub[16];
         for (int j = 0; j < kSimtK; j++) sub[j] = 0;

@@ -31,9 +31,8 @@ struct TransmmLaunch {
     uint8_t col_local[16];    // local tile bit of column bit c
     uint64_t piece_off[32];       // 512-thread piece tables (SIMT kernel)
     uint32_t piece_slot[32];
-    // tensor-core kernels: the tile runs as sub-tiles with its top column bits
-    // fixed (m = 6: 2 sub-tiles of 64 x 64; m = 7: 4 of 128 x 16), pipelined
-    // through three staging buffers
+    // 6-qubit tensor-core kernel: the tile runs as 2 sub-tiles of 64 x 64 with
+    // its top column bit fixed, pipelined through three staging buffers
     uint8_t sub_phys[12];         // physical bit of sub-tile local bit j
     uint8_t row_sub[8];           // sub-tile local bit of row bit r
     uint8_t col_sub[8];           // sub-tile local bit of column bit c
