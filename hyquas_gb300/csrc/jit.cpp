@@ -16,6 +16,7 @@
 
 #include <dlfcn.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <functional>
@@ -144,11 +145,75 @@ struct Gen {
               << (k1 ? "true" : "false") << ");\n";
     }
 
+    // Per-slot signed scales within a phase: register vector j (and its
+    // imaginary partner) holds sigma_j = (neg_j ? -1 : 1) sqrt(2)^e_j times its
+    // true amplitudes.  Exact 45-degree phases (T, T^dagger) then cost one add
+    // per component, the slot's scale growing by sqrt 2, and the adds of H,
+    // sqrt(X) and sqrt(Y) absorb a scale ratio as one FMA; the phase's closing
+    // multiply divides every slot by its scale.
+    std::vector<int> se;
+    std::vector<char> sn;
+    void reset_scales() {
+        se.assign(nv, 0);
+        sn.assign(nv, 0);
+    }
+    double sigma(int j) const {
+        double r = std::ldexp(1.0, se[j] >= 0 ? se[j] / 2 : -((-se[j]) / 2));
+        if (se[j] & 1) r = se[j] > 0 ? r * std::sqrt(2.0) : r / std::sqrt(2.0);
+        return (sn[j] ? -1.0 : 1.0) * r;
+    }
+    // sigma_a / sigma_b, exact for even exponent differences
+    double ratio(int a, int b) const {
+        const int d = se[a] - se[b];
+        double r = std::ldexp(1.0, d >= 0 ? d / 2 : -((-d) / 2));
+        if (d & 1) r = d > 0 ? r * std::sqrt(2.0) : r / std::sqrt(2.0);
+        return (sn[a] != sn[b] ? -1.0 : 1.0) * r;
+    }
+    static std::string vconst(double x) { return "vdup(" + flit((float)x) + ")"; }
+    // base + k * other as one instruction
+    static std::string comb(const std::string& base, double k, const std::string& other) {
+        if (k == 1.0) return "vadd(" + base + ", " + other + ")";
+        if (k == -1.0) return "vsub(" + base + ", " + other + ")";
+        return "vfma(" + vconst(k) + ", " + other + ", " + base + ")";
+    }
+    // give slot h the scale of slot j (two multiplies)
+    void align(int j, int h) {
+        if (se[h] == se[j] && sn[h] == sn[j]) return;
+        const std::string k = vconst(ratio(j, h));
+        o << R(h) << " = vmul(" << k << ", " << R(h) << "); " << I(h) << " = vmul(" << k << ", " << I(h)
+          << ");\n";
+        se[h] = se[j];
+        sn[h] = sn[j];
+    }
+
+    // scaled forms: sqrt(X) / sqrt(Y) keep both scales, so they also run under a
+    // run-time control; H and X change them, so only unconditionally
+    static bool pair_fast(int kind, bool full, bool has_cout) {
+        return (full && !has_cout && (kind == OP_H || kind == OP_X)) ||
+               (full && (kind == OP_SY || kind == OP_SX));
+    }
+    static bool pair_needs_align(int kind, bool full, bool has_cout) {
+        if (kind == OP_U || kind == OP_REAL || kind == OP_IMOFF) return true;
+        if (kind == OP_H || kind == OP_SY || kind == OP_SX || kind == OP_X)
+            return !pair_fast(kind, full, has_cout);
+        return false;
+    }
+
     bool uses_neg = false;  // phase has sign-only factors outside the register set
     void op(const OshmOp& op, bool& uses_acc) {
         const int kind = op.kind, J = op.tbit;
         const float* m = op.m;
         const bool has_cout = (op.flags & OPF_COUT) != 0;
+        // slots an op combines at their plain values are given equal scales
+        // first, outside any run-time control (the scales are compile-time facts)
+        if (kind != OP_DOUT && J >= 1) {
+            for (int j = 0; j < nv; j++) {
+                if (j & (1 << (J - 1))) continue;
+                bool k0, k1;
+                lanes(op.creg, j, k0, k1);
+                if ((k0 || k1) && pair_needs_align(kind, k0 && k1, has_cout)) align(j, j | (1 << (J - 1)));
+            }
+        }
         if (has_cout) o << "if ((pidx & " << hex64(op.cout) << ") == " << hex64(op.cout) << ") {\n";
         o << "{\n";
         if (kind == OP_DOUT) {
@@ -284,14 +349,58 @@ struct Gen {
             if (negf_op) o << "x ^= 0x8000000080000000ull; y ^= 0x8000000080000000ull; ";
             o << x << " = x; " << y << " = y; }\n";
         };
+        // DROT by an odd multiple of pi/4 (T, T^dagger): d1 = m6 + i m7 with |m6| = |m7|
+        const double h2 = std::sqrt(0.5);
+        const bool rot45 = kind == OP_DROT && !has_cout && std::fabs(std::fabs(m[6]) - h2) < 1e-6 &&
+                           std::fabs(std::fabs(m[7]) - h2) < 1e-6;
         for (int j = 0; j < nv; j++) {
             if (j & (1 << (J - 1))) continue;
             const int h = j | (1 << (J - 1));
             bool k0, k1;
             lanes(op.creg, j, k0, k1);
             if (!k0 && !k1) continue;
+            const bool full = k0 && k1;
+            const bool fast = pair_fast(kind, full, has_cout);
             o << "{ const v2 lr = " << R(j) << ", li = " << I(j) << ", hr = " << R(h) << ", hi = " << I(h)
               << ";\n";
+            if (fast && (kind == OP_H || kind == OP_SY || kind == OP_SX)) {
+                const double rj = ratio(j, h), rh = ratio(h, j);
+                if (kind == OP_H) {  // L' = L + H, H' = L - H (stored as H - L, scale negated)
+                    o << R(j) << " = " << comb("lr", rj, "hr") << "; " << I(j) << " = " << comb("li", rj, "hi")
+                      << "; " << R(h) << " = " << comb("hr", -rh, "lr") << "; " << I(h) << " = "
+                      << comb("hi", -rh, "li") << ";\n";
+                    sn[h] = !sn[h];
+                } else if (kind == OP_SY) {  // L' = L - H, H' = L + H
+                    o << R(j) << " = " << comb("lr", -rj, "hr") << "; " << I(j) << " = "
+                      << comb("li", -rj, "hi") << "; " << R(h) << " = " << comb("hr", rh, "lr") << "; " << I(h)
+                      << " = " << comb("hi", rh, "li") << ";\n";
+                } else {  // L' = L - i H, H' = H - i L
+                    o << R(j) << " = " << comb("lr", rj, "hi") << "; " << I(j) << " = "
+                      << comb("li", -rj, "hr") << "; " << R(h) << " = " << comb("hr", rh, "li") << "; " << I(h)
+                      << " = " << comb("hi", -rh, "lr") << ";\n";
+                }
+                o << "}\n";
+                continue;
+            }
+            if (fast && kind == OP_X) {
+                o << R(j) << " = hr; " << I(j) << " = hi; " << R(h) << " = lr; " << I(h) << " = li;\n}\n";
+                std::swap(se[j], se[h]);
+                std::swap(sn[j], sn[h]);
+                continue;
+            }
+            if (full && rot45) {
+                // (x, y) -> (c x - s y, s x + c y) sqrt 2, c, s = +-1; c = -1 is stored negated
+                const double c = m[6] > 0 ? 1.0 : -1.0, sgn = m[7] > 0 ? 1.0 : -1.0;
+                if (c > 0)
+                    o << R(h) << " = " << comb("hr", -sgn, "hi") << "; " << I(h) << " = " << comb("hi", sgn, "hr")
+                      << ";\n}\n";
+                else
+                    o << R(h) << " = " << comb("hr", sgn, "hi") << "; " << I(h) << " = " << comb("hi", -sgn, "hr")
+                      << ";\n}\n";
+                se[h] += 1;
+                if (c < 0) sn[h] = !sn[h];
+                continue;
+            }
             switch (kind) {
                 case OP_U:
                     assign(R(j), "vfma(bin, hi, vfma(b, hr, vfma(ain, li, vmul(a, lr))))", "lr", k0, k1);
@@ -510,6 +619,7 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
         o << "float2 acc = make_float2(1.f, 0.f);\n(void)acc;\nbool negf = false;\n(void)negf;\n";
         bool uses_acc = false;
         g.uses_neg = false;
+        g.reset_scales();
         for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) g.op(prog.ops[oi], uses_acc);
         if (g.uses_neg && uses_acc) {
             o << "if (negf) { acc.x = -acc.x; acc.y = -acc.y; }\n";
@@ -520,19 +630,38 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
                 o << "r" << j << " ^= 0x8000000080000000ull; i" << j << " ^= 0x8000000080000000ull;\n";
             o << "}\n";
         }
-        if (uses_acc || P.scale != 1.f) {
-            o << "{ float2 f = acc;\n";
-            if (P.scale != 1.f) o << "f.x *= " << flit(P.scale) << "; f.y *= " << flit(P.scale) << ";\n";
-            o << "const v2 fr = vdup(f.x), fi = vdup(f.y), fin = vdup(-f.y);\n";
-            if (uses_acc) {
-                for (int j = 0; j < NV; j++)
-                    o << "{ const v2 a = r" << j << ", b = i" << j << "; r" << j
-                      << " = vfma(fin, b, vmul(fr, a)); i" << j << " = vfma(fi, a, vmul(fr, b)); }\n";
-            } else {
-                for (int j = 0; j < NV; j++)
-                    o << "r" << j << " = vmul(fr, r" << j << "); i" << j << " = vmul(fr, i" << j << ");\n";
+        // closing multiply: the phase's deferred scale and the per-thread factor,
+        // each slot divided by its own scale
+        std::vector<double> kf(NV);
+        bool any_k = false;
+        for (int j = 0; j < NV; j++) {
+            kf[j] = double(P.scale) / g.sigma(j);
+            any_k = any_k || (float)kf[j] != 1.f;
+        }
+        if (uses_acc) {
+            o << "{ const float2 f = acc;\n";
+            std::map<float, int> names;
+            for (int j = 0; j < NV; j++) {
+                const float k = (float)kf[j];
+                auto it = names.find(k);
+                if (it == names.end()) {
+                    const int q = (int)names.size();
+                    names[k] = q;
+                    o << "const v2 fr" << q << " = vdup(f.x * " << flit(k) << "), fi" << q << " = vdup(f.y * "
+                      << flit(k) << "), fin" << q << " = vdup(-f.y * " << flit(k) << ");\n";
+                }
+                const int q = names[k];
+                o << "{ const v2 a = r" << j << ", b = i" << j << "; r" << j << " = vfma(fin" << q
+                  << ", b, vmul(fr" << q << ", a)); i" << j << " = vfma(fi" << q << ", a, vmul(fr" << q
+                  << ", b)); }\n";
             }
             o << "}\n";
+        } else if (any_k) {
+            for (int j = 0; j < NV; j++) {
+                if ((float)kf[j] == 1.f) continue;
+                o << "r" << j << " = vmul(" << Gen::vconst(kf[j]) << ", r" << j << "); i" << j << " = vmul("
+                  << Gen::vconst(kf[j]) << ", i" << j << ");\n";
+            }
         }
         if (lastp) {
             // vector j holds the amplitudes at pidx | (its register bits) and + 1

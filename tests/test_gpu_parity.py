@@ -260,6 +260,69 @@ def test_transmm_qft_precision_sweep(hq, oracle, prec, k):
     assert r["max_abs_err"] <= tol and r["one_minus_fidelity"] <= fid, r
 
 
+def clifford_t_circuit(seed, n, count):
+    """Gates the generated kernels run in closed form: H, sqrt(X) / sqrt(Y) as
+    RX / RY(pi/2), T, T^dagger, S, X, Z and their controlled forms, CZ."""
+    rng = W.SplitMix64(seed)
+    half = math.pi / 2
+    out = []
+    for _ in range(count):
+        qs = rng.shuffle(range(n))[:3]
+        k = rng.below(12)
+        if k == 0:
+            out.append((W.H, qs[0], -1, -1, ()))
+        elif k == 1:
+            out.append((W.RX, qs[0], -1, -1, (half,)))
+        elif k == 2:
+            out.append((W.RY, qs[0], -1, -1, (half,)))
+        elif k == 3:
+            out.append((W.T, qs[0], -1, -1, ()))
+        elif k == 4:
+            out.append((W.TDG, qs[0], -1, -1, ()))
+        elif k == 5:
+            out.append((W.S, qs[0], -1, -1, ()))
+        elif k == 6:
+            out.append((W.X, qs[0], -1, -1, ()))
+        elif k == 7:
+            out.append((W.CZ, qs[1], qs[0], -1, ()))
+        elif k == 8:
+            out.append((W.CNOT, qs[1], qs[0], -1, ()))
+        elif k == 9:
+            out.append((W.CRX, qs[1], qs[0], -1, (half,)))
+        elif k == 10:
+            out.append((W.CU1, qs[1], qs[0], -1, (math.pi / 4,)))
+        else:
+            out.append((W.U1, qs[0], -1, -1, (-3 * math.pi / 4,)))
+    return out
+
+
+@pytest.mark.parametrize("n,seed", [(14, 1), (17, 2), (20, 3)])
+def test_generated_kernels_clifford_t(hq, oracle, n, seed):
+    """Closed-form gates in the generated kernels (per-vector scales: T as one add
+    per component, H / sqrt(X) / sqrt(Y) absorbing scale ratios) against the oracle."""
+    desc = clifford_t_circuit(700 + seed, n, 600)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile("oshm")
+    psi = W.random_state(40 + seed, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    c.run_on(s)
+    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+
+
+@pytest.mark.parametrize("rows,cols", [(4, 4), (3, 6)])
+def test_grid_circuit_small_vs_oracle(hq, oracle, rows, cols):
+    n = rows * cols
+    desc = W.grid_random(5, rows, cols, 20)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile("oshm")
+    s = hq.State(n)
+    c.run_on(s)
+    check(oracle, oracle.run_f64(n, desc), s.store())
+
+
 def inverse(desc):
     inv = {W.T: W.TDG, W.TDG: W.T, W.S: W.SDG, W.SDG: W.S}
     out = []
