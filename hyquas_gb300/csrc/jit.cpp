@@ -361,6 +361,10 @@ struct Gen {
             if (!k0 && !k1) continue;
             const bool full = k0 && k1;
             const bool fast = pair_fast(kind, full, has_cout);
+            if (kind == OP_NEGHI && full && !has_cout) {  // a sign: folded into the slot's scale
+                sn[h] = !sn[h];
+                continue;
+            }
             o << "{ const v2 lr = " << R(j) << ", li = " << I(j) << ", hr = " << R(h) << ", hi = " << I(h)
               << ";\n";
             if (fast && (kind == OP_H || kind == OP_SY || kind == OP_SX)) {
@@ -621,15 +625,6 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
         g.uses_neg = false;
         g.reset_scales();
         for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) g.op(prog.ops[oi], uses_acc);
-        if (g.uses_neg && uses_acc) {
-            o << "if (negf) { acc.x = -acc.x; acc.y = -acc.y; }\n";
-        } else if (g.uses_neg) {
-            // a sign: flip the sign bits (ALU pipe) of every amplitude
-            o << "if (negf) {\n";
-            for (int j = 0; j < NV; j++)
-                o << "r" << j << " ^= 0x8000000080000000ull; i" << j << " ^= 0x8000000080000000ull;\n";
-            o << "}\n";
-        }
         // closing multiply: the phase's deferred scale and the per-thread factor,
         // each slot divided by its own scale
         std::vector<double> kf(NV);
@@ -637,6 +632,16 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
         for (int j = 0; j < NV; j++) {
             kf[j] = double(P.scale) / g.sigma(j);
             any_k = any_k || (float)kf[j] != 1.f;
+        }
+        const bool neg_in_mul = g.uses_neg && !uses_acc && any_k;  // the sign rides on the multiply
+        if (g.uses_neg && uses_acc) {
+            o << "if (negf) { acc.x = -acc.x; acc.y = -acc.y; }\n";
+        } else if (g.uses_neg && !neg_in_mul) {
+            // a sign: flip the sign bits (ALU pipe) of every amplitude
+            o << "if (negf) {\n";
+            for (int j = 0; j < NV; j++)
+                o << "r" << j << " ^= 0x8000000080000000ull; i" << j << " ^= 0x8000000080000000ull;\n";
+            o << "}\n";
         }
         if (uses_acc) {
             o << "{ const float2 f = acc;\n";
@@ -655,6 +660,12 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
                   << ", b, vmul(fr" << q << ", a)); i" << j << " = vfma(fi" << q << ", a, vmul(fr" << q
                   << ", b)); }\n";
             }
+            o << "}\n";
+        } else if (neg_in_mul) {
+            o << "{ const float ns = negf ? -1.f : 1.f;\n";
+            for (int j = 0; j < NV; j++)
+                o << "{ const v2 k = vdup(" << flit((float)kf[j]) << " * ns); r" << j << " = vmul(k, r" << j
+                  << "); i" << j << " = vmul(k, i" << j << "); }\n";
             o << "}\n";
         } else if (any_k) {
             for (int j = 0; j < NV; j++) {
