@@ -348,6 +348,7 @@ def run_plain20(args, dist: Dist):
     circ.addGates(gates)
     circ.compile("plain")
     state = hq.State(n)
+    circ.capture_graph(state)  # one kernel node per gate: replays without a host launch per gate
     flush = hq.State(28)  # 2 GiB written between steps: the state is L2-sized
     for _ in range(args.warmup):
         state.init_zero()

@@ -400,10 +400,10 @@ double circuit_run(hq_circuit_s* c, hq_state_s* s, bool sync) {
         HQ_CHECK_CUDA(cudaEventCreate(&c->ev1));
     }
     HQ_CHECK_CUDA(cudaEventRecord(c->ev0, st));
-    if (c->opt.backend == HQ_BACKEND_PLAIN || c->n < 6) {
-        apply_plain(s, c->folded);
-    } else if (c->graph && c->graph_state == s) {
+    if (c->graph && c->graph_state == s) {
         HQ_CHECK_CUDA(cudaGraphLaunch(c->graph, st));
+    } else if (c->opt.backend == HQ_BACKEND_PLAIN || c->n < 6) {
+        apply_plain(s, c->folded);
     } else {
         circuit_launch_groups(c, s->d, st);
     }
@@ -455,8 +455,11 @@ void circuit_profile(hq_circuit_s* c, hq_state_s* s, double* group_us) {
 void circuit_capture(hq_circuit_s* c, hq_state_s* s) {
     HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
     HQ_REQUIRE(s->n == c->n, HQ_ERR_INVALID, "state/circuit size mismatch");
-    if (c->opt.backend == HQ_BACKEND_PLAIN || c->n < 6) return;  // nothing to capture
+    const bool plain = c->opt.backend == HQ_BACKEND_PLAIN || c->n < 6;
     cudaStream_t st = ctx().stream;
+    // runs start from the canonical layout, so the captured launches (plain
+    // gates are lowered through the layout) are the ones every run makes
+    state_canonicalize(s);
     HQ_CHECK_CUDA(cudaStreamSynchronize(st));
     if (c->graph) {
         cudaGraphExecDestroy(c->graph);
@@ -465,7 +468,10 @@ void circuit_capture(hq_circuit_s* c, hq_state_s* s) {
     cudaGraph_t g = nullptr;
     HQ_CHECK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
-        circuit_launch_groups(c, s->d, st);
+        if (plain)
+            apply_plain(s, c->folded);  // one kernel node per gate
+        else
+            circuit_launch_groups(c, s->d, st);
     } catch (...) {
         cudaStreamEndCapture(st, &g);
         if (g) cudaGraphDestroy(g);

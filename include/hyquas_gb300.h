@@ -237,7 +237,9 @@ hq_status hq_circuit_profile(hq_circuit c, hq_state s, double* group_us);
 /* Enqueue the compiled schedule on the library stream without synchronising. */
 hq_status hq_circuit_enqueue(hq_circuit c, hq_state s);
 /* Capture the compiled schedule for state s into a CUDA graph (replayed by
- * later hq_circuit_run / hq_circuit_enqueue calls on the same state). */
+ * later hq_circuit_run / hq_circuit_enqueue calls on the same state).  Plain-
+ * path circuits are captured too: one kernel node per gate, no host launch per
+ * gate on replay. */
 hq_status hq_circuit_capture_graph(hq_circuit c, hq_state s);
 hq_status hq_synchronize(void);
 

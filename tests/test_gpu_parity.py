@@ -51,6 +51,24 @@ def test_plain_config1_u3_cnot_n20(hq, oracle):
     assert abs(s.norm() - 1.0) < 1e-5
 
 
+@pytest.mark.parametrize("backend", ["plain", "oshm"])
+def test_graph_replay_matches_direct_run(hq, oracle, backend):
+    """A captured CUDA graph replays the compiled schedule (for the plain path one
+    kernel node per gate), including SWAPs folded into the layout."""
+    n = 16
+    desc = W.plain_u3_cnot(3, n, 6)
+    desc = desc[:40] + [(W.SWAP, 2, 9, -1, ())] + desc[40:]
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile(backend)
+    s = hq.State(n)
+    c.capture_graph(s)
+    for _ in range(3):
+        s.init_zero()
+        c.run_on(s)
+    check(oracle, oracle.run_f64(n, desc), s.store())
+
+
 @pytest.mark.parametrize("t", ALL_TYPES)
 def test_plain_every_gate_type(hq, oracle, t):
     n = 9
