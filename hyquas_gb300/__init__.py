@@ -111,6 +111,10 @@ def _load():
         "hq_plan_groups": [I32, P, I32, C.POINTER(hq_compile_options), C.POINTER(I32), P, P, P, P,
                            P, P],
         "hq_circuit_capture_graph": [P, P],
+        "hq_circuit_serialize": [P, P, U64, C.POINTER(U64)],
+        "hq_plan_serialize": [I32, P, I32, C.POINTER(hq_compile_options), P, U64, C.POINTER(U64)],
+        "hq_schedule_inspect": [P, U64, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32), P, P, P, P],
+        "hq_circuit_deserialize": [P, U64, C.POINTER(P)],
         "hq_synchronize": [],
         "hq_apply_oshm_group": [P, P, I32, U64],
         "hq_apply_transmm_group": [P, P, I32, U64, I32],
@@ -308,6 +312,45 @@ def gate_array(gates) -> C.Array:
     return arr
 
 
+def _compile_options(backend="oshm", tile_qubits=0, coalesce=0, mm_qubits=0, precision="bf16x3",
+                     reference_grouping=False, specialize=2) -> hq_compile_options:
+    o = hq_compile_options()
+    check(lib.hq_compile_options_default(C.byref(o)))
+    o.backend = _BACKENDS[backend] if isinstance(backend, str) else backend
+    o.tile_qubits = tile_qubits
+    o.coalesce = coalesce
+    o.mm_qubits = mm_qubits
+    o.mm_precision = _PRECISIONS[precision] if isinstance(precision, str) else precision
+    o.reference_grouping = 1 if reference_grouping else 0
+    o.specialize = specialize
+    return o
+
+
+def plan_schedule(num_qubits: int, gates, **options) -> bytes:
+    """Host only: the schedule bytes compile would make for these gates (the
+    reference's Schedule::serialize, src/schedule.cpp:156-325)."""
+    arr = gate_array(gates)
+    o = _compile_options(**options)
+    n = C.c_uint64()
+    check(lib.hq_plan_serialize(num_qubits, arr, len(gates), C.byref(o), None, 0, C.byref(n)))
+    buf = C.create_string_buffer(n.value)
+    check(lib.hq_plan_serialize(num_qubits, arr, len(gates), C.byref(o), buf, n.value, C.byref(n)))
+    return buf.raw[:n.value]
+
+
+def inspect_schedule(data: bytes) -> dict:
+    """Host only: check schedule bytes and list their groups."""
+    nq, ngates, ng = C.c_int32(), C.c_int32(), C.c_int32()
+    check(lib.hq_schedule_inspect(data, len(data), C.byref(nq), C.byref(ngates), C.byref(ng),
+                                  None, None, None, None))
+    k = max(1, ng.value)
+    b, g, w = (C.c_int32 * k)(), (C.c_int32 * k)(), (C.c_int32 * k)()
+    r = (C.c_uint64 * k)()
+    check(lib.hq_schedule_inspect(data, len(data), None, None, None, b, g, w, r))
+    return {"num_qubits": nq.value, "num_gates": ngates.value,
+            "groups": [(b[i], g[i], w[i], r[i]) for i in range(ng.value)]}
+
+
 def cost_params() -> dict:
     """The cost model's constants (seconds per amplitude per pass, and per launch)."""
     p = hq_cost_params()
@@ -490,6 +533,30 @@ class Circuit:
         c.addGates(gates)
         return c
 
+    @classmethod
+    def deserialize(cls, data: bytes) -> "Circuit":
+        """A compiled circuit from schedule bytes (no partitioning)."""
+        h = C.c_void_p()
+        check(lib.hq_circuit_deserialize(data, len(data), C.byref(h)))
+        nq = C.c_int32()
+        check(lib.hq_schedule_inspect(data, len(data), C.byref(nq), None, None, None, None, None,
+                                      None))
+        c = cls.__new__(cls)
+        c.numQubits = nq.value
+        c._h = h
+        c.state = None
+        c.result = None
+        c.gates = []
+        return c
+
+    def serialize(self) -> bytes:
+        """The compiled schedule as bytes (Schedule::serialize, src/schedule.cpp:156-325)."""
+        n = C.c_uint64()
+        check(lib.hq_circuit_serialize(self._h, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        check(lib.hq_circuit_serialize(self._h, buf, n.value, C.byref(n)))
+        return buf.raw[:n.value]
+
     @property
     def handle(self):
         return self._h
@@ -506,15 +573,8 @@ class Circuit:
     def compile(self, backend: str | int = "oshm", tile_qubits: int = 0, coalesce: int = 0,
                 mm_qubits: int = 0, precision: str | int = "bf16x3", reference_grouping: bool = False,
                 specialize: int = 2):
-        o = hq_compile_options()
-        check(lib.hq_compile_options_default(C.byref(o)))
-        o.backend = _BACKENDS[backend] if isinstance(backend, str) else backend
-        o.tile_qubits = tile_qubits
-        o.coalesce = coalesce
-        o.mm_qubits = mm_qubits
-        o.mm_precision = _PRECISIONS[precision] if isinstance(precision, str) else precision
-        o.reference_grouping = 1 if reference_grouping else 0
-        o.specialize = specialize
+        o = _compile_options(backend, tile_qubits, coalesce, mm_qubits, precision, reference_grouping,
+                             specialize)
         check(lib.hq_circuit_compile(self._h, C.byref(o)))
 
     def schedule(self):

@@ -388,6 +388,83 @@ hq_status hq_plan_groups(int32_t n, const hq_gate* gates, int32_t num_gates,
     HQ_API_END
 }
 
+namespace {
+hq_status copy_out(const std::vector<uint8_t>& b, void* buf, uint64_t cap, uint64_t* len) {
+    *len = b.size();
+    if (!buf) return HQ_OK;  // size query
+    HQ_REQUIRE(cap >= b.size(), HQ_ERR_INVALID, "buffer of %llu bytes, schedule needs %zu",
+               (unsigned long long)cap, b.size());
+    std::memcpy(buf, b.data(), b.size());
+    return HQ_OK;
+}
+}  // namespace
+
+hq_status hq_circuit_serialize(hq_circuit c, void* buf, uint64_t cap, uint64_t* len) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_NONNULL(len);
+    copy_out(schedule_serialize(c), buf, cap, len);
+    HQ_API_END
+}
+
+hq_status hq_plan_serialize(int32_t n, const hq_gate* gates, int32_t num_gates,
+                            const hq_compile_options* opt, void* buf, uint64_t cap, uint64_t* len) {
+    HQ_API_BEGIN
+    HQ_NONNULL(len);
+    HQ_REQUIRE(n >= 1 && n <= 36, HQ_ERR_INVALID, "num_qubits %d out of range [1,36]", n);
+    HQ_REQUIRE(num_gates >= 0 && (num_gates == 0 || gates), HQ_ERR_INVALID, "bad gate list");
+    hq_compile_options o;
+    if (opt)
+        o = *opt;
+    else
+        hq_compile_options_default(&o);
+    hq_circuit_s c;
+    c.n = n;
+    for (int32_t i = 0; i < num_gates; i++) {
+        validate_gate(gates[i], n);
+        c.gates.push_back(gates[i]);
+    }
+    circuit_plan(&c, o);
+    c.compiled = true;  // the plan is all the bytes hold
+    copy_out(schedule_serialize(&c), buf, cap, len);
+    HQ_API_END
+}
+
+hq_status hq_schedule_inspect(const void* buf, uint64_t len, int32_t* num_qubits, int32_t* num_gates,
+                              int32_t* num_groups, int32_t* backend, int32_t* gates_per_group,
+                              int32_t* width, uint64_t* related) {
+    HQ_API_BEGIN
+    hq_circuit_s c;
+    schedule_deserialize(static_cast<const uint8_t*>(buf), (size_t)len, &c);
+    if (num_qubits) *num_qubits = c.n;
+    if (num_gates) *num_gates = (int32_t)c.gates.size();
+    if (num_groups) *num_groups = (int32_t)c.part.groups.size();
+    for (size_t i = 0; i < c.part.groups.size(); i++) {
+        const GroupPlan& gp = c.part.groups[i];
+        if (backend) backend[i] = gp.backend;
+        if (gates_per_group) gates_per_group[i] = (int32_t)gp.gates.size();
+        if (width) width[i] = gp.width;
+        if (related) related[i] = gp.related;
+    }
+    HQ_API_END
+}
+
+hq_status hq_circuit_deserialize(const void* buf, uint64_t len, hq_circuit* out) {
+    HQ_API_BEGIN
+    HQ_NONNULL(out);
+    std::unique_ptr<hq_circuit_s> c(new hq_circuit_s());
+    schedule_deserialize(static_cast<const uint8_t*>(buf), (size_t)len, c.get());
+    ensure_init();
+    try {
+        circuit_lower(c.get());
+    } catch (...) {
+        circuit_release(c.get());
+        throw;
+    }
+    *out = c.release();
+    HQ_API_END
+}
+
 hq_status hq_circuit_program_bytes(hq_circuit c, uint64_t* bytes) {
     HQ_API_BEGIN
     HQ_NONNULL(c);

@@ -269,9 +269,7 @@ uint64_t oshm_tile_mask(const GroupPlan& gp, int n) {
     return tile;
 }
 
-void circuit_compile(hq_circuit_s* c, const hq_compile_options& o) {
-    circuit_release(c);
-    ensure_init();
+void circuit_plan(hq_circuit_s* c, const hq_compile_options& o) {
     const int n = c->n;
     c->opt = o;
     // SWAP folding: drop swaps, relabel the gates after them
@@ -297,13 +295,21 @@ void circuit_compile(hq_circuit_s* c, const hq_compile_options& o) {
         c->part = Partition();
         c->part.final_pos.resize(n);
         for (int q = 0; q < n; q++) c->part.final_pos[q] = q;
-        c->compiled = true;
         return;
     }
     std::vector<int> id(n);
     for (int q = 0; q < n; q++) id[q] = q;
     c->part = partition(n, c->folded, id, cfg);
+}
 
+void circuit_lower(hq_circuit_s* c) {
+    const int n = c->n;
+    const hq_compile_options& o = c->opt;
+    if (o.backend == HQ_BACKEND_PLAIN || n < 6) {
+        c->compiled = true;
+        return;
+    }
+    CompileConfig cfg = config_from_options(o, n);
     std::vector<OshmPhase> phases;
     std::vector<OshmOp> ops;
     std::vector<double> umats;
@@ -374,6 +380,13 @@ void circuit_compile(hq_circuit_s* c, const hq_compile_options& o) {
         }
     }
     c->compiled = true;
+}
+
+void circuit_compile(hq_circuit_s* c, const hq_compile_options& o) {
+    circuit_release(c);
+    ensure_init();
+    circuit_plan(c, o);
+    circuit_lower(c);
 }
 
 void circuit_launch_groups(hq_circuit_s* c, void* state, cudaStream_t st) {

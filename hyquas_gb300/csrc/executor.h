@@ -85,6 +85,15 @@ void apply_oshm_group(hq_state_s* s, const std::vector<hq_gate>& gates, uint64_t
 CompileConfig config_from_options(const hq_compile_options& o, int n);
 uint64_t oshm_tile_mask(const GroupPlan& gp, int n);
 void circuit_compile(hq_circuit_s* c, const hq_compile_options& opt);
+// the two halves of compile: the host plan (SWAP folding, fusion for the
+// interpreter, partition) and the device lowering (phases, fused unitaries,
+// uploads, generated kernels) of the plan already in `c`
+void circuit_plan(hq_circuit_s* c, const hq_compile_options& opt);
+void circuit_lower(hq_circuit_s* c);
+// compiled-schedule bytes (schedule_io.cpp)
+std::vector<uint8_t> schedule_serialize(const hq_circuit_s* c);
+// parse and check `len` bytes into c's plan (gates, options, partition); no device work
+void schedule_deserialize(const uint8_t* buf, size_t len, hq_circuit_s* c);
 double circuit_run(hq_circuit_s* c, hq_state_s* s, bool sync);
 void circuit_capture(hq_circuit_s* c, hq_state_s* s);
 void circuit_profile(hq_circuit_s* c, hq_state_s* s, double* group_us);

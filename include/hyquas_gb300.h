@@ -223,6 +223,28 @@ hq_status hq_plan_groups(int32_t num_qubits, const hq_gate* gates, int32_t num_g
                          const hq_compile_options* opt, int32_t* num_groups, int32_t* backend,
                          int32_t* gates_per_group, int32_t* width, uint64_t* related,
                          int32_t* phases, int32_t* gate_order);
+/* ---- compiled-schedule bytes (the reference serialises its Schedule for
+ * broadcast: Schedule/GateGroup/State::serialize, src/schedule.cpp:156-325;
+ * Gate::serialize, src/gate.cpp:558-589) ----------------------------------
+ * The bytes hold the compile options, the gates, the SWAP-folded gates and
+ * the partition, with a checksum.  *len receives the size; buf = NULL asks for
+ * the size only, otherwise cap must be at least *len. */
+hq_status hq_circuit_serialize(hq_circuit c, void* buf, uint64_t cap, uint64_t* len);
+/* Host only: plan num_gates gates as hq_circuit_compile would and write the
+ * schedule bytes (no device needed). */
+hq_status hq_plan_serialize(int32_t num_qubits, const hq_gate* gates, int32_t num_gates,
+                            const hq_compile_options* opt, void* buf, uint64_t cap, uint64_t* len);
+/* Host only: check schedule bytes (magic, version, checksum, every size and
+ * index) and report the register size, gate count and, per group, backend,
+ * gate count, width and related-qubit mask (arrays may be NULL, else they need
+ * num_groups entries; size them with a first call that passes NULL). */
+hq_status hq_schedule_inspect(const void* buf, uint64_t len, int32_t* num_qubits, int32_t* num_gates,
+                              int32_t* num_groups, int32_t* backend, int32_t* gates_per_group,
+                              int32_t* width, uint64_t* related);
+/* A compiled circuit from schedule bytes: the partitioner does not run; the
+ * groups are lowered and uploaded as compile would.  Invalid bytes give
+ * HQ_ERR_INVALID (HQ_ERR_UNSUPPORTED for another format version). */
+hq_status hq_circuit_deserialize(const void* buf, uint64_t len, hq_circuit* out);
 /* Bytes of device-resident program (gate-group lowering, fused unitaries)
  * that compile uploaded for this circuit. */
 hq_status hq_circuit_program_bytes(hq_circuit c, uint64_t* bytes);

@@ -69,6 +69,44 @@ def test_graph_replay_matches_direct_run(hq, oracle, backend):
     check(oracle, oracle.run_f64(n, desc), s.store())
 
 
+@pytest.mark.parametrize("backend,opts", [("oshm", {}), ("oshm", {"specialize": 0}), ("hybrid", {}),
+                                          ("transmm", {"mm_qubits": 7}), ("plain", {})])
+def test_serialized_schedule_runs_the_same(hq, oracle, backend, opts):
+    """Schedule bytes (Schedule::serialize, src/schedule.cpp:156-325) give a
+    circuit that runs exactly as the one compiled, without partitioning; bytes
+    planned on the host load the same way."""
+    n = 16
+    desc = W.grid_random(6, 4, 4, 12)
+    desc = desc[:50] + [(W.SWAP, 3, 12, -1, ())] + desc[50:]
+    gates = W.to_gates(desc)
+    c = hq.Circuit(n)
+    c.addGates(gates)
+    c.compile(backend, **opts)
+    psi = W.random_state(61, n)
+    s1 = hq.State(n, zero=False)
+    s1.load(psi)
+    c.run_on(s1)
+    data = c.serialize()
+    c2 = hq.Circuit.deserialize(data)
+    assert c2.schedule() == c.schedule()
+    s2 = hq.State(n, zero=False)
+    s2.load(psi)
+    c2.run_on(s2)
+    assert np.array_equal(s1.store(), s2.store())
+    c3 = hq.Circuit.deserialize(hq.plan_schedule(n, gates, backend=backend, **opts))
+    s3 = hq.State(n, zero=False)
+    s3.load(psi)
+    c3.run_on(s3)
+    assert np.array_equal(s1.store(), s3.store())
+    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s1.store(),
+          tol=5e-5 if backend == "transmm" else TOL)
+
+
+def test_deserialize_refuses_bad_bytes(hq):
+    with pytest.raises(hq.HQError):
+        hq.Circuit.deserialize(b"HQSC" + bytes(20))
+
+
 @pytest.mark.parametrize("t", ALL_TYPES)
 def test_plain_every_gate_type(hq, oracle, t):
     n = 9
