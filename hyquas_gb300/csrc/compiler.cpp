@@ -740,6 +740,9 @@ double cost_transmm(int n, int m, int precision) {
     const double amps = double(uint64_t(1) << n);
     double per = precision == HQ_MM_FP32 ? c.mm_fp32 : (precision == HQ_MM_TF32 ? c.mm_tf32 : c.mm_bf16x3);
     if (precision == HQ_MM_FP32 && m > 6) per *= double(1 << (m - 6));  // SIMT flops grow with 2^m
+    // tensor cores: 6 and 7 qubits cost the same per pass; 8 streams its 512 KB
+    // unitary through shared memory per tile (measured 3.1x the 7-qubit pass)
+    if (precision != HQ_MM_FP32 && m > 7) per *= 3.1;
     return amps * per + c.launch;
 }
 

@@ -243,7 +243,9 @@ CompileConfig config_from_options(const hq_compile_options& o, int n) {
     cfg.reference = o.reference_grouping != 0;
     cfg.tile = o.tile_qubits > 0 ? o.tile_qubits : 13;
     cfg.coalesce = o.coalesce > 0 ? o.coalesce : 3;
-    cfg.mm_qubits = o.mm_qubits > 0 ? o.mm_qubits : 6;
+    // tensor-core passes cost the same at 6 and 7 qubits (measured), so the
+    // wider group is the default there; FP32 SIMT doubles its cost per qubit
+    cfg.mm_qubits = o.mm_qubits > 0 ? o.mm_qubits : (o.mm_precision == HQ_MM_FP32 ? 6 : 7);
     cfg.mm_precision = o.mm_precision;
     HQ_REQUIRE(o.backend == HQ_BACKEND_PLAIN || o.backend == HQ_BACKEND_OSHM ||
                    o.backend == HQ_BACKEND_TRANSMM || o.backend == HQ_BACKEND_HYBRID,

@@ -185,7 +185,8 @@ typedef struct hq_compile_options {
     int32_t backend;       /* hq_backend */
     int32_t tile_qubits;   /* OShareMem tile width k (0 = autotuned) */
     int32_t coalesce;      /* low physical qubits always in a tile (0 = default) */
-    int32_t mm_qubits;     /* TransMM group width (0 = autotuned, else 4..8) */
+    int32_t mm_qubits;     /* TransMM group width, 4..8 (0 = 7 on the tensor cores, 6 for
+                              FP32 SIMT) */
     int32_t mm_precision;  /* hq_mm_precision */
     int32_t reference_grouping; /* 1 = use the reference's widths (tile 10, coalesce 3, MAT 6) */
     int32_t specialize;    /* OShareMem kernels: 0 = interpreter (runs of single-qubit gates
