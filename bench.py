@@ -263,7 +263,7 @@ def run_ours(args, dist: Dist):
     achieved = bytes_per_pass / (np.mean(dom) * 1e-6) / 1e9 if dom else None
     traffic = None
     tfile = ROOT / "profiles" / "oshm_grid30_traffic.json"
-    if tfile.exists():
+    if tfile.exists() and oshm_t and n == 30:  # the capture covers the OShareMem kernel at 30 qubits
         traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
