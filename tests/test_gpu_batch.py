@@ -122,7 +122,7 @@ def test_batch_rejects_mismatch(hq):
         b.run()  # not compiled
 
 
-def test_batch_config4_full(hq, oracle):
+def test_batch_512_circuits_full(hq, oracle):
     """The 512-circuit workload (n 10-22, depth 8-40): every state normalised,
     a sample of circuits bit-for-bit equal to their solo runs, the smallest ones
     against the oracle."""

@@ -42,7 +42,7 @@ def random_circuit(seed, n, count, types=ALL_TYPES, qubits=None):
     return desc
 
 
-def test_plain_config1_u3_cnot_n20(hq, oracle):
+def test_plain_u3_cnot_n20(hq, oracle):
     n = 20
     desc = W.plain_u3_cnot(1, n, 10)
     s = hq.State(n)
