@@ -84,6 +84,8 @@ def _load():
         "hq_state_init_zero": [P],
         "hq_state_load": [P, P],
         "hq_state_store": [P, P],
+        "hq_state_store_async": [P, P],
+        "hq_state_wait": [P],
         "hq_state_amps": [P, P, I64, P],
         "hq_state_layout": [P, P],
         "hq_state_num_qubits": [P, C.POINTER(I32)],
@@ -424,6 +426,18 @@ class State:
         assert out.dtype == np.complex64 and out.size == (1 << self.n) and out.flags.c_contiguous
         check(lib.hq_state_store(self._h, out.ctypes.data))
         return out
+
+    def store_async(self, out: np.ndarray) -> np.ndarray:
+        """Start the readback into `out` (pinned memory for full speed) and
+        return at once; `wait()` before reading `out`."""
+        assert out.dtype == np.complex64 and out.size == (1 << self.n) and out.flags.c_contiguous
+        check(lib.hq_state_store_async(self._h, out.ctypes.data))
+        self._pending_out = out  # kept alive until the copy lands
+        return out
+
+    def wait(self):
+        check(lib.hq_state_wait(self._h))
+        self._pending_out = None
 
     def amps(self, idx) -> np.ndarray:
         idx = np.ascontiguousarray(idx, dtype=np.uint64)

@@ -208,6 +208,7 @@ void batch_compile(hq_batch_s* b, const hq_compile_options* opt) {
 // the persistent launch.
 static void batch_enqueue_work(hq_batch_s* b, bool zero_init, cudaStream_t st) {
     for (BatchEntry& e : b->entries) {
+        state_wait_copy(e.s);
         if (zero_init) {
             for (int q = 0; q < e.n; q++) e.s->pos[q] = q;  // contents are rewritten
             if (e.ngroups == 0) launch_init_zero(e.s->d, e.n, st);
@@ -243,6 +244,7 @@ void batch_enqueue(hq_batch_s* b, bool zero_init) {
     cudaStream_t st = ctx().stream;
     if (b->graph && b->graph_zero == zero_init && !b->stall_next) {
         for (BatchEntry& e : b->entries) {
+            state_wait_copy(e.s);
             if (!zero_init) state_canonicalize(e.s);
         }
         HQ_CHECK_CUDA(cudaGraphLaunch(b->graph, st));

@@ -119,6 +119,7 @@ hq_status hq_state_destroy(hq_state s) {
 hq_status hq_state_init_zero(hq_state s) {
     HQ_API_BEGIN
     HQ_NONNULL(s);
+    state_wait_copy(s);
     launch_init_zero(s->d, s->n, ctx().stream);
     for (int q = 0; q < s->n; q++) s->pos[q] = q;
     HQ_CHECK_CUDA(cudaStreamSynchronize(ctx().stream));
@@ -129,6 +130,7 @@ hq_status hq_state_load(hq_state s, const float* host) {
     HQ_API_BEGIN
     HQ_NONNULL(s);
     HQ_NONNULL(host);
+    state_wait_copy(s);
     HQ_CHECK_CUDA(cudaMemcpyAsync(s->d, host, s->bytes, cudaMemcpyHostToDevice, ctx().stream));
     for (int q = 0; q < s->n; q++) s->pos[q] = q;
     HQ_CHECK_CUDA(cudaStreamSynchronize(ctx().stream));
@@ -142,6 +144,21 @@ hq_status hq_state_store(hq_state s, float* host) {
     state_canonicalize(s);
     HQ_CHECK_CUDA(cudaMemcpyAsync(host, s->d, s->bytes, cudaMemcpyDeviceToHost, ctx().stream));
     HQ_CHECK_CUDA(cudaStreamSynchronize(ctx().stream));
+    HQ_API_END
+}
+
+hq_status hq_state_store_async(hq_state s, float* host) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    HQ_NONNULL(host);
+    state_store_async(s, host);
+    HQ_API_END
+}
+
+hq_status hq_state_wait(hq_state s) {
+    HQ_API_BEGIN
+    HQ_NONNULL(s);
+    state_wait_host(s);
     HQ_API_END
 }
 
@@ -234,6 +251,7 @@ hq_status hq_state_remap(hq_state s, const int32_t* new_pos) {
 hq_status hq_apply_gates(hq_state s, const hq_gate* gates, int32_t num_gates) {
     HQ_API_BEGIN
     HQ_NONNULL(s);
+    state_wait_copy(s);
     HQ_REQUIRE(num_gates >= 0, HQ_ERR_INVALID, "negative gate count");
     if (num_gates == 0) return HQ_OK;
     HQ_NONNULL(gates);
@@ -777,6 +795,7 @@ hq_status hq_apply_oshm_group(hq_state s, const hq_gate* gates, int32_t num_gate
                               uint64_t tile_mask) {
     HQ_API_BEGIN
     HQ_NONNULL(s);
+    state_wait_copy(s);
     HQ_REQUIRE(num_gates >= 0 && (num_gates == 0 || gates), HQ_ERR_INVALID, "bad gate list");
     std::vector<hq_gate> v(gates, gates + num_gates);
     apply_oshm_group(s, v, tile_mask);

@@ -80,6 +80,28 @@ void dev_free(void* p, size_t bytes) {
     c.in_use = c.in_use >= bytes ? c.in_use - bytes : 0;
 }
 
+void* dev_alloc_ordered(size_t bytes) {
+    Context& c = ctx();
+    if (c.budget && c.in_use + bytes > c.budget)
+        fail(HQ_ERR_NOMEM, "allocation of %zu bytes exceeds the HBM budget (%llu of %llu in use)",
+             bytes, (unsigned long long)c.in_use, (unsigned long long)c.budget);
+    void* p = nullptr;
+    cudaError_t e = cudaMallocAsync(&p, bytes, c.stream);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        fail(HQ_ERR_NOMEM, "cudaMallocAsync(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    c.in_use += bytes;
+    return p;
+}
+
+void dev_free_ordered(void* p, size_t bytes) {
+    if (!p) return;
+    Context& c = ctx();
+    cudaFreeAsync(p, c.stream);
+    c.in_use = c.in_use >= bytes ? c.in_use - bytes : 0;
+}
+
 void check_device_error() {
     Context& c = ctx();
     int h[4];

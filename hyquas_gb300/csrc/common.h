@@ -47,6 +47,7 @@ struct Context {
     uint64_t budget = 0;  // 0 = no budget
     uint64_t in_use = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // asynchronous readbacks (made on first use)
     int* d_error = nullptr;        // device error word (bounded waits, bad indices)
     double* d_partials = nullptr;  // reduction partials (FP64), see k_plain.cu
     size_t partials_cap = 0;       // doubles
@@ -58,6 +59,11 @@ Context& ctx();               // initialises on first use (device 0 unless hq_in
 void ensure_init();
 void* dev_alloc(size_t bytes);  // budget-checked cudaMalloc
 void dev_free(void* p, size_t bytes);
+// stream-ordered on the library stream (cudaMallocAsync / cudaFreeAsync): for
+// memory only the library stream uses, so that freeing it does not wait for
+// other streams (an asynchronous readback, say) the way cudaFree does
+void* dev_alloc_ordered(size_t bytes);
+void dev_free_ordered(void* p, size_t bytes);
 void check_device_error();      // reads and clears the device error word
 
 inline int popcount64(uint64_t x) { return __builtin_popcountll(x); }

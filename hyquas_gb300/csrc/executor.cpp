@@ -39,12 +39,16 @@ hq_state_s* state_create(int n) {
 
 void state_destroy(hq_state_s* s) {
     if (!s) return;
+    if (s->copy_pending) cudaEventSynchronize(s->copy_done);
+    if (s->ready) cudaEventDestroy(s->ready);
+    if (s->copy_done) cudaEventDestroy(s->copy_done);
     if (s->d) dev_free(s->d, s->bytes);
     if (s->d_scratch) dev_free(s->d_scratch, sizeof(double) * s->scratch_doubles);
     delete s;
 }
 
 void state_remap(hq_state_s* s, const std::vector<int>& np) {
+    state_wait_copy(s);
     const int n = s->n;
     HQ_REQUIRE((int)np.size() == n, HQ_ERR_INVALID, "remap: layout size");
     std::vector<char> seen(n, 0);
@@ -63,6 +67,29 @@ void state_remap(hq_state_s* s, const std::vector<int>& np) {
         s->pos[q2] = s->pos[q];
         s->pos[q] = np[q];
     }
+}
+
+void state_wait_copy(hq_state_s* s) {
+    if (s->copy_pending) HQ_CHECK_CUDA(cudaStreamWaitEvent(ctx().stream, s->copy_done, 0));
+}
+
+void state_store_async(hq_state_s* s, void* host) {
+    state_canonicalize(s);
+    Context& c = ctx();
+    if (!c.copy_stream) HQ_CHECK_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+    if (!s->ready) HQ_CHECK_CUDA(cudaEventCreateWithFlags(&s->ready, cudaEventDisableTiming));
+    if (!s->copy_done) HQ_CHECK_CUDA(cudaEventCreateWithFlags(&s->copy_done, cudaEventDisableTiming));
+    HQ_CHECK_CUDA(cudaEventRecord(s->ready, c.stream));
+    HQ_CHECK_CUDA(cudaStreamWaitEvent(c.copy_stream, s->ready, 0));
+    HQ_CHECK_CUDA(cudaMemcpyAsync(host, s->d, s->bytes, cudaMemcpyDeviceToHost, c.copy_stream));
+    HQ_CHECK_CUDA(cudaEventRecord(s->copy_done, c.copy_stream));
+    s->copy_pending = true;
+}
+
+void state_wait_host(hq_state_s* s) {
+    if (!s->copy_pending) return;
+    HQ_CHECK_CUDA(cudaEventSynchronize(s->copy_done));
+    s->copy_pending = false;
 }
 
 void state_canonicalize(hq_state_s* s) {
@@ -84,17 +111,17 @@ void state_gather(hq_state_s* s, const uint64_t* idx, int64_t count, float* out)
     }
     cudaStream_t st = ctx().stream;
     const size_t ib = sizeof(uint64_t) * count, ob = sizeof(float) * 2 * count;
-    char* buf = (char*)dev_alloc(ib + ob);
+    char* buf = (char*)dev_alloc_ordered(ib + ob);
     try {
         HQ_CHECK_CUDA(cudaMemcpyAsync(buf, phys.data(), ib, cudaMemcpyHostToDevice, st));
         launch_gather(s->d, (const uint64_t*)buf, count, buf + ib, st);
         HQ_CHECK_CUDA(cudaMemcpyAsync(out, buf + ib, ob, cudaMemcpyDeviceToHost, st));
         HQ_CHECK_CUDA(cudaStreamSynchronize(st));
     } catch (...) {
-        dev_free(buf, ib + ob);
+        dev_free_ordered(buf, ib + ob);
         throw;
     }
-    dev_free(buf, ib + ob);
+    dev_free_ordered(buf, ib + ob);
 }
 
 void state_marginals(hq_state_s* s, double* h) {
@@ -137,7 +164,7 @@ void state_sample(hq_state_s* s, int shots, uint64_t seed, uint64_t* out) {
     const int n = s->n;
     const size_t nb = sample_scratch_doubles(n);
     const size_t bytes = sizeof(double) * nb + sizeof(uint64_t) * size_t(std::max(shots, 1));
-    char* buf = (char*)dev_alloc(bytes);
+    char* buf = (char*)dev_alloc_ordered(bytes);
     cudaStream_t st = ctx().stream;
     std::vector<uint64_t> phys(size_t(std::max(shots, 1)));
     double total = 0.0;
@@ -151,10 +178,10 @@ void state_sample(hq_state_s* s, int shots, uint64_t seed, uint64_t* out) {
                                           cudaMemcpyDeviceToHost, st));
         HQ_CHECK_CUDA(cudaStreamSynchronize(st));
     } catch (...) {
-        dev_free(buf, bytes);
+        dev_free_ordered(buf, bytes);
         throw;
     }
-    dev_free(buf, bytes);
+    dev_free_ordered(buf, bytes);
     HQ_REQUIRE(total > 0.0, HQ_ERR_STATE, "sample: the state has zero norm");
     for (int i = 0; i < shots; i++) {
         uint64_t l = 0;
@@ -196,7 +223,7 @@ void apply_oshm_group(hq_state_s* s, const std::vector<hq_gate>& gates, uint64_t
     // ops start on a 256-byte boundary: OshmOp holds 64-bit fields
     const size_t pb = (sizeof(OshmPhase) * std::max<size_t>(1, prog.phases.size()) + 255) & ~size_t(255);
     const size_t ob = sizeof(OshmOp) * std::max<size_t>(1, prog.ops.size());
-    char* buf = (char*)dev_alloc(pb + ob);
+    char* buf = (char*)dev_alloc_ordered(pb + ob);
     cudaStream_t st = ctx().stream;
     try {
         HQ_CHECK_CUDA(cudaMemcpyAsync(buf, prog.phases.data(), sizeof(OshmPhase) * prog.phases.size(),
@@ -208,10 +235,10 @@ void apply_oshm_group(hq_state_s* s, const std::vector<hq_gate>& gates, uint64_t
         launch_oshm(p, st);
         HQ_CHECK_CUDA(cudaStreamSynchronize(st));
     } catch (...) {
-        dev_free(buf, pb + ob);
+        dev_free_ordered(buf, pb + ob);
         throw;
     }
-    dev_free(buf, pb + ob);
+    dev_free_ordered(buf, pb + ob);
     check_device_error();
 }
 
@@ -221,10 +248,10 @@ void circuit_release(hq_circuit_s* c) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     c->graph = nullptr;
     c->graph_state = nullptr;
-    if (c->d_phases) dev_free(c->d_phases, c->phases_bytes);
-    if (c->d_ops) dev_free(c->d_ops, c->ops_bytes);
-    if (c->d_umats) dev_free(c->d_umats, c->umats_bytes);
-    if (c->d_mm_scratch) dev_free(c->d_mm_scratch, c->mm_scratch_bytes);
+    if (c->d_phases) dev_free_ordered(c->d_phases, c->phases_bytes);
+    if (c->d_ops) dev_free_ordered(c->d_ops, c->ops_bytes);
+    if (c->d_umats) dev_free_ordered(c->d_umats, c->umats_bytes);
+    if (c->d_mm_scratch) dev_free_ordered(c->d_mm_scratch, c->mm_scratch_bytes);
     c->d_phases = nullptr;
     c->d_ops = nullptr;
     c->d_umats = nullptr;
@@ -339,18 +366,18 @@ void circuit_lower(hq_circuit_s* c) {
     cudaStream_t st = ctx().stream;
     if (!phases.empty()) {
         c->phases_bytes = sizeof(OshmPhase) * phases.size();
-        c->d_phases = (OshmPhase*)dev_alloc(c->phases_bytes);
+        c->d_phases = (OshmPhase*)dev_alloc_ordered(c->phases_bytes);
         HQ_CHECK_CUDA(cudaMemcpyAsync(c->d_phases, phases.data(), c->phases_bytes,
                                       cudaMemcpyHostToDevice, st));
     }
     if (!ops.empty()) {
         c->ops_bytes = sizeof(OshmOp) * ops.size();
-        c->d_ops = (OshmOp*)dev_alloc(c->ops_bytes);
+        c->d_ops = (OshmOp*)dev_alloc_ordered(c->ops_bytes);
         HQ_CHECK_CUDA(cudaMemcpyAsync(c->d_ops, ops.data(), c->ops_bytes, cudaMemcpyHostToDevice, st));
     }
     if (!umats.empty()) {
         c->umats_bytes = sizeof(double) * umats.size();
-        c->d_umats = (double*)dev_alloc(c->umats_bytes);
+        c->d_umats = (double*)dev_alloc_ordered(c->umats_bytes);
         HQ_CHECK_CUDA(cudaMemcpyAsync(c->d_umats, umats.data(), c->umats_bytes,
                                       cudaMemcpyHostToDevice, st));
     }

@@ -18,6 +18,10 @@ struct hq_state_s {
     std::vector<int> pos;       // logical -> physical
     double* d_scratch = nullptr;  // reduction partials (FP64)
     size_t scratch_doubles = 0;
+    // asynchronous readback (state_store_async): the copy runs on the library's
+    // copy stream; work that writes the state first waits for copy_done
+    cudaEvent_t ready = nullptr, copy_done = nullptr;
+    bool copy_pending = false;
 };
 
 namespace hq {
@@ -72,6 +76,12 @@ namespace hq {
 hq_state_s* state_create(int n);
 void state_destroy(hq_state_s* s);
 void state_canonicalize(hq_state_s* s);
+// the library stream waits for a pending asynchronous readback of s (before writing s)
+void state_wait_copy(hq_state_s* s);
+// canonical-order device -> host copy on the copy stream; returns at once
+void state_store_async(hq_state_s* s, void* host);
+// block until s's asynchronous readback has landed in host memory
+void state_wait_host(hq_state_s* s);
 void state_remap(hq_state_s* s, const std::vector<int>& new_pos);
 void state_gather(hq_state_s* s, const uint64_t* logical_idx, int64_t count, float* out);
 void state_marginals(hq_state_s* s, double* h_out);  // [total, p1(phys bit b)]

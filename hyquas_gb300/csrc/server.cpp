@@ -197,6 +197,10 @@ void grow_dev(char*& p, size_t& cap, size_t need, cudaStream_t st) {
 void free_request_memory(hq_server_s* sv, Request* r) {
     cudaStream_t st = sv->stream;
     if (r->state) {
+        // a caller's asynchronous readback of the borrowed state finishes first
+        if (r->state->copy_pending) HQ_CHECK_CUDA(cudaStreamWaitEvent(st, r->state->copy_done, 0));
+        if (r->state->ready) cudaEventDestroy(r->state->ready);
+        if (r->state->copy_done) cudaEventDestroy(r->state->copy_done);
         if (r->state->d) cudaFreeAsync(r->state->d, st);
         if (r->state->d_scratch) cudaFreeAsync(r->state->d_scratch, st);
         delete r->state;

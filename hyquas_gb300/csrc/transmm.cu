@@ -443,21 +443,21 @@ void transmm_finalize(hq_circuit_s* c) {
     }
     if (u_off == 0) return;
     c->umats_bytes = sizeof(double) * u_off;
-    c->d_umats = (double*)dev_alloc(c->umats_bytes);
+    c->d_umats = (double*)dev_alloc_ordered(c->umats_bytes);
     c->mm_scratch_bytes = op_off;
-    c->d_mm_scratch = dev_alloc(op_off);
+    c->d_mm_scratch = dev_alloc_ordered(op_off);
     for (DeviceGroup& dg : c->dgroups) {
         if (dg.backend != HQ_BACKEND_TRANSMM) continue;
         std::vector<ComposeGate> cg = to_compose(dg.phys_gates, dg.mm_rows);
         const size_t gb = sizeof(ComposeGate) * std::max<size_t>(1, cg.size());
-        ComposeGate* d_g = (ComposeGate*)dev_alloc(gb);
+        ComposeGate* d_g = (ComposeGate*)dev_alloc_ordered(gb);
         HQ_CHECK_CUDA(cudaMemcpyAsync(d_g, cg.data(), sizeof(ComposeGate) * cg.size(),
                                       cudaMemcpyHostToDevice, st));
         launch_compose(dg.mm_m, d_g, (int)cg.size(), c->d_umats + dg.umat_off, st);
         prepare_operand(dg.mm_m, dg.mm_precision, c->d_umats + dg.umat_off,
                         (char*)c->d_mm_scratch + dg.operand_off, st);
         HQ_CHECK_CUDA(cudaStreamSynchronize(st));
-        dev_free(d_g, gb);
+        dev_free_ordered(d_g, gb);
     }
 }
 
@@ -471,21 +471,22 @@ void transmm_launch(hq_circuit_s* c, const DeviceGroup& dg, void* state, cudaStr
 
 void compose_unitary(int m, const std::vector<ComposeGate>& gates, double* d_u, cudaStream_t st) {
     const size_t gb = sizeof(ComposeGate) * std::max<size_t>(1, gates.size());
-    ComposeGate* d_g = (ComposeGate*)dev_alloc(gb);
+    ComposeGate* d_g = (ComposeGate*)dev_alloc_ordered(gb);
     try {
         HQ_CHECK_CUDA(cudaMemcpyAsync(d_g, gates.data(), sizeof(ComposeGate) * gates.size(),
                                       cudaMemcpyHostToDevice, st));
         launch_compose(m, d_g, (int)gates.size(), d_u, st);
         HQ_CHECK_CUDA(cudaStreamSynchronize(st));
     } catch (...) {
-        dev_free(d_g, gb);
+        dev_free_ordered(d_g, gb);
         throw;
     }
-    dev_free(d_g, gb);
+    dev_free_ordered(d_g, gb);
 }
 
 void apply_unitary_device(hq_state_s* s, const double* d_u, int m, uint64_t rows_phys,
                           int precision) {
+    state_wait_copy(s);
     cudaStream_t st = ctx().stream;
     uint64_t rows = rows_phys, tile;
     HQ_REQUIRE(__builtin_popcountll(rows) == m, HQ_ERR_INVALID, "row mask/width mismatch");
@@ -495,7 +496,7 @@ void apply_unitary_device(hq_state_s* s, const double* d_u, int m, uint64_t rows
     tile = rows;
     for (int b = 0; b < s->n && __builtin_popcountll(tile) < kSimtK; b++) tile |= uint64_t(1) << b;
     const size_t ob = operand_bytes(m, precision);
-    void* d_op = dev_alloc(ob);
+    void* d_op = dev_alloc_ordered(ob);
     try {
         prepare_operand(m, precision, d_u, d_op, st);
         TransmmLaunch p = make_launch(s->n, m, rows, tile, precision);
@@ -505,10 +506,10 @@ void apply_unitary_device(hq_state_s* s, const double* d_u, int m, uint64_t rows
         launch_any(p, st);
         HQ_CHECK_CUDA(cudaStreamSynchronize(st));
     } catch (...) {
-        dev_free(d_op, ob);
+        dev_free_ordered(d_op, ob);
         throw;
     }
-    dev_free(d_op, ob);
+    dev_free_ordered(d_op, ob);
     check_device_error();
 }
 
@@ -557,15 +558,15 @@ extern "C" hq_status hq_group_unitary(const hq_gate* gates, int32_t num_gates, u
     for (auto& g : v) validate_gate(g, 64);
     std::vector<ComposeGate> cg = to_compose(v, group_mask);
     const size_t ub = sizeof(double) * (size_t(2) << (2 * m));
-    double* d_u = (double*)dev_alloc(ub);
+    double* d_u = (double*)dev_alloc_ordered(ub);
     try {
         compose_unitary(m, cg, d_u, ctx().stream);
         HQ_CHECK_CUDA(cudaMemcpy(out, d_u, ub, cudaMemcpyDeviceToHost));
     } catch (...) {
-        dev_free(d_u, ub);
+        dev_free_ordered(d_u, ub);
         throw;
     }
-    dev_free(d_u, ub);
+    dev_free_ordered(d_u, ub);
     HQ_API_CATCH
 }
 
@@ -589,15 +590,15 @@ extern "C" hq_status hq_apply_transmm_group(hq_state s, const hq_gate* gates, in
     const int m = __builtin_popcountll(rows);
     std::vector<ComposeGate> cg = to_compose(phys, rows);
     const size_t ub = sizeof(double) * (size_t(2) << (2 * m));
-    double* d_u = (double*)dev_alloc(ub);
+    double* d_u = (double*)dev_alloc_ordered(ub);
     try {
         compose_unitary(m, cg, d_u, ctx().stream);
         apply_unitary_device(s, d_u, m, rows, precision);
     } catch (...) {
-        dev_free(d_u, ub);
+        dev_free_ordered(d_u, ub);
         throw;
     }
-    dev_free(d_u, ub);
+    dev_free_ordered(d_u, ub);
     HQ_API_CATCH
 }
 
@@ -670,14 +671,14 @@ extern "C" hq_status hq_apply_unitary(hq_state s, const double* unitary, uint64_
         u.swap(pu);
     }
     const size_t ub = sizeof(double) * u.size();
-    double* d_u = (double*)dev_alloc(ub);
+    double* d_u = (double*)dev_alloc_ordered(ub);
     try {
         HQ_CHECK_CUDA(cudaMemcpy(d_u, u.data(), ub, cudaMemcpyHostToDevice));
         apply_unitary_device(s, d_u, pm, prow, precision);
     } catch (...) {
-        dev_free(d_u, ub);
+        dev_free_ordered(d_u, ub);
         throw;
     }
-    dev_free(d_u, ub);
+    dev_free_ordered(d_u, ub);
     HQ_API_CATCH
 }

@@ -120,6 +120,14 @@ hq_status hq_state_load(hq_state s, const float* host_amps);
  * device first).  kernelDeviceToHost + Circuit::ampAt, src/kernelSimple.cu:523-525,
  * src/circuit.cpp:54-64, 115-118. */
 hq_status hq_state_store(hq_state s, float* host_amps);
+/* The same copy without waiting: it runs on the library's copy stream after
+ * the work already queued on s, so a circuit on another state overlaps it.
+ * host_amps must stay valid (and should be pinned, hq_host_alloc) until
+ * hq_state_wait(s); later work that writes s waits for the copy on the device.
+ * hq_state_store's asynchronous form, for pipelined readback. */
+hq_status hq_state_store_async(hq_state s, float* host_amps);
+/* Block until s's pending asynchronous copy has landed in host memory. */
+hq_status hq_state_wait(hq_state s);
 /* Download the amplitudes at `count` logical indices.  Circuit::ampAtGPU /
  * kernelGetAmp, src/circuit.cpp:120-142, src/kernelSimple.cu:518-522. */
 hq_status hq_state_amps(hq_state s, const uint64_t* logical_idx, int64_t count, float* out);

@@ -102,6 +102,38 @@ def test_serialized_schedule_runs_the_same(hq, oracle, backend, opts):
           tol=5e-5 if backend == "transmm" else TOL)
 
 
+def test_async_readback_orders_with_later_writes(hq, oracle):
+    """hq_state_store_async: the copy holds the state as it was when it was
+    queued, even when a circuit, an init or a load writes the state right after;
+    a circuit on another state runs meanwhile."""
+    n = 20
+    d1 = W.grid_random(7, 4, 5, 10)
+    d2 = W.plain_u3_cnot(5, n, 4)
+    c1, c2 = hq.Circuit(n), hq.Circuit(n)
+    c1.addGates(W.to_gates(d1))
+    c2.addGates(W.to_gates(d2))
+    c1.compile("oshm")
+    c2.compile("oshm")
+    a, b = hq.State(n), hq.State(n)
+    bufs = [hq.PinnedBuffer(1 << n) for _ in range(3)]
+    c1.run_on(a)
+    a.store_async(bufs[0].array)
+    c2.run_on(a)                       # writes a: waits for the copy on the device
+    c2.run_on(b)                       # another state: free to overlap
+    b.store_async(bufs[1].array)
+    a.store_async(bufs[2].array)
+    a.init_zero()
+    a.wait()
+    b.wait()
+    r1 = oracle.run_f64(n, d1)
+    check(oracle, r1, bufs[0].array.copy())
+    check(oracle, oracle.apply_f64(n, r1, d2), bufs[2].array.copy())
+    check(oracle, oracle.run_f64(n, d2), bufs[1].array.copy())
+    assert abs(a.amps([0])[0] - 1) < 1e-7
+    for x in bufs:
+        x.free()
+
+
 def test_deserialize_refuses_bad_bytes(hq):
     with pytest.raises(hq.HQError):
         hq.Circuit.deserialize(b"HQSC" + bytes(20))
