@@ -219,9 +219,29 @@ public:
     hq_circuit handle() const { return c_; }
     hq_state state() const { return s_; }  // the device state after run(destroy = false)
 
+    // The compiled schedule as bytes (the reference's Schedule::serialize,
+    // src/schedule.cpp:156-325), and a compiled Circuit back from them: the
+    // partitioner does not run again.
+    std::vector<unsigned char> serialize() const {
+        uint64_t len = 0;
+        check(hq_circuit_serialize(c_, nullptr, 0, &len));
+        std::vector<unsigned char> b(static_cast<size_t>(len));
+        check(hq_circuit_serialize(c_, b.data(), len, &len));
+        return b;
+    }
+    static std::unique_ptr<Circuit> deserialize(const std::vector<unsigned char>& b) {
+        int32_t n = 0;
+        check(hq_schedule_inspect(b.data(), b.size(), &n, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                  nullptr));
+        hq_circuit h = nullptr;
+        check(hq_circuit_deserialize(b.data(), b.size(), &h));
+        return std::unique_ptr<Circuit>(new Circuit(n, h));
+    }
+
     const int numQubits;
 
 private:
+    Circuit(int n, hq_circuit h) : numQubits(n), c_(h) {}
     hq_circuit c_ = nullptr;
     hq_state s_ = nullptr;
     std::vector<Gate> gates_;

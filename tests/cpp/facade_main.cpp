@@ -76,6 +76,30 @@ int main(int argc, char** argv) {
         }
         return 0;
     }
+    if (argc >= 4 && std::strcmp(argv[1], "roundtrip") == 0) {
+        // compile, serialise, load the bytes into a second Circuit, run both
+        const int n = std::atoi(argv[2]);
+        unsigned long long s = std::strtoull(argv[3], nullptr, 10);
+        Circuit c(n);
+        for (int layer = 0; layer < 4; layer++) {
+            for (int q = 0; q < n; q++) c.addGate(Gate::U3(q, uni(s), uni(s), uni(s)));
+            for (int q = layer & 1; q + 1 < n; q += 2) c.addGate(Gate::CNOT(q, q + 1));
+        }
+        c.compile();
+        const std::vector<unsigned char> bytes = c.serialize();
+        std::unique_ptr<Circuit> d = Circuit::deserialize(bytes);
+        c.run();
+        d->run();
+        for (qindex i = 0; i < (qindex(1) << n); i++) {
+            const ResultItem a = c.ampAt(i), b = d->ampAt(i);
+            if (a.amp.x != b.amp.x || a.amp.y != b.amp.y) {
+                std::printf("mismatch at %lld\n", (long long)i);
+                return 2;
+            }
+        }
+        std::printf("ok %zu bytes\n", bytes.size());
+        return 0;
+    }
     if (argc >= 3 && std::strcmp(argv[1], "qasm") == 0) {
         std::unique_ptr<Circuit> c = parse_circuit(argv[2]);
         c->dumpGates();

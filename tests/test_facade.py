@@ -66,3 +66,12 @@ def test_facade_circuit_matches_oracle(facade_bin, oracle, n):
             desc.append((W.CNOT, q + 1, q, -1, ()))
     c = oracle.compare(oracle.run_f64(n, desc), got)
     assert c["max_abs_err"] <= 1e-5 and c["one_minus_fidelity"] <= 1e-6, c
+
+
+@pytest.mark.gpu
+def test_facade_schedule_round_trip(facade_bin):
+    """Circuit::serialize / Circuit::deserialize through the C++ facade: the
+    loaded circuit gives the same amplitudes, bit for bit."""
+    txt = subprocess.run([str(facade_bin), "roundtrip", "14", "9"], check=True, capture_output=True,
+                         text=True).stdout
+    assert txt.startswith("ok "), txt
