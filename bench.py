@@ -279,6 +279,9 @@ def run_ours(args, dist: Dist):
     if not args.no_e2e:
         states = [state, hq.State(n)]
         pinned = [hq.PinnedBuffer(1 << n), hq.PinnedBuffer(1 << n)]
+        tr = time.perf_counter()
+        states[1].store(pinned[1].array)  # the host link's readback rate, for the record
+        readback_gbs = 8.0 * (1 << n) / (time.perf_counter() - tr) / 1e9
         h2d = 0
         t0 = time.perf_counter()
         for i in range(args.steps):
@@ -296,7 +299,8 @@ def run_ours(args, dist: Dist):
         e2e_s = dist.max(time.perf_counter() - t0)
         e2e = {"value": dist.ws * args.steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(8 * (1 << n)),
-               "readback": "asynchronous, two states alternating"}
+               "readback": "asynchronous, two states alternating",
+               "readback_gbs": readback_gbs}
         states[1].free()
         for b in pinned:
             b.free()

@@ -134,6 +134,24 @@ def test_async_readback_orders_with_later_writes(hq, oracle):
         x.free()
 
 
+def test_large_pinned_buffer_readback(hq):
+    """Pinned buffers of 64 MiB and more are mapped on the GPU's NUMA node and
+    registered in place; synchronous and asynchronous readbacks into one match
+    a readback into ordinary memory."""
+    n = 24
+    s = hq.State(n, zero=False)
+    s.load(W.random_state(3, n))
+    buf = hq.PinnedBuffer(1 << n)
+    s.store(buf.array)
+    plain = s.store()
+    assert np.array_equal(buf.array, plain)
+    buf.array[:] = 0
+    s.store_async(buf.array)
+    s.wait()
+    assert np.array_equal(buf.array, plain)
+    buf.free()
+
+
 def test_deserialize_refuses_bad_bytes(hq):
     with pytest.raises(hq.HQError):
         hq.Circuit.deserialize(b"HQSC" + bytes(20))
