@@ -283,24 +283,32 @@ def run_ours(args, dist: Dist):
         states[1].store(pinned[1].array)  # the host link's readback rate, for the record
         readback_gbs = 8.0 * (1 << n) / (time.perf_counter() - tr) / 1e9
         h2d = 0
+        parts = []  # per step: compile, init + run, queue + release (ms)
         t0 = time.perf_counter()
         for i in range(args.steps):
             st = states[i % 2]
+            ta = time.perf_counter()
             c2 = hq.Circuit(n)
             c2.addGates(gates)
             c2.compile(backend=args.backend)
             h2d = c2.program_bytes()
+            tb = time.perf_counter()
             st.init_zero()
             c2.run_on(st)
+            tc = time.perf_counter()
             st.store_async(pinned[i % 2].array)
             del c2
+            parts.append([round((tb - ta) * 1e3, 1), round((tc - tb) * 1e3, 1),
+                          round((time.perf_counter() - tc) * 1e3, 1)])
         for st in states:
             st.wait()
         e2e_s = dist.max(time.perf_counter() - t0)
         e2e = {"value": dist.ws * args.steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(8 * (1 << n)),
                "readback": "asynchronous, two states alternating",
-               "readback_gbs": readback_gbs}
+               "readback_gbs": readback_gbs,
+               "step_parts_ms": {"compile": [p[0] for p in parts], "init_run": [p[1] for p in parts],
+                                 "queue_release": [p[2] for p in parts]}}
         states[1].free()
         for b in pinned:
             b.free()
