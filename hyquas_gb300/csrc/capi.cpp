@@ -2,13 +2,7 @@
 // per-gate path, compiled circuits and their executor, FP64 readout.
 #include <cuda_runtime.h>
 
-#include <sys/mman.h>
-#include <sys/syscall.h>
-#include <unistd.h>
-
 #include <algorithm>
-#include <map>
-#include <mutex>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -83,68 +77,18 @@ hq_status hq_hbm_in_use(uint64_t* bytes) {
     HQ_API_END
 }
 
-// Page-locked host buffers on the GPU's own NUMA node: on a host with several
-// CPU sockets a buffer on another socket's memory crosses the CPU-CPU link on
-// every transfer.  Large buffers are mapped, given a preference for the GPU's
-// node (mbind), placed by first touch and pinned in place; anything else, or
-// a host that reports no node, gets cudaHostAlloc.
-namespace {
-std::mutex g_host_mu;
-std::map<void*, size_t> g_host_mapped;  // buffers made by mmap + cudaHostRegister
-
-void* numa_local_pinned(size_t bytes, int node) {
-    void* p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
-    if (p == MAP_FAILED) return nullptr;
-    unsigned long mask[16] = {0};  // 1024 nodes
-    if (node < 1024) {
-        mask[node / 64] |= 1ul << (node % 64);
-        (void)syscall(SYS_mbind, p, bytes, 1 /* MPOL_PREFERRED */, mask, 1025ul, 0u);  // best effort
-    }
-    std::memset(p, 0, bytes);  // first touch places the pages
-    if (cudaHostRegister(p, bytes, cudaHostRegisterDefault) != cudaSuccess) {
-        (void)cudaGetLastError();
-        munmap(p, bytes);
-        return nullptr;
-    }
-    std::lock_guard<std::mutex> lk(g_host_mu);
-    g_host_mapped[p] = bytes;
-    return p;
-}
-}  // namespace
-
 hq_status hq_host_alloc(uint64_t bytes, void** out) {
     HQ_API_BEGIN
     HQ_NONNULL(out);
     ensure_init();
     *out = nullptr;
-    int node = -1;
-    if (cudaDeviceGetAttribute(&node, cudaDevAttrHostNumaId, ctx().device) != cudaSuccess) {
-        (void)cudaGetLastError();
-        node = -1;
-    }
-    if (node >= 0 && bytes >= (uint64_t(64) << 20)) *out = numa_local_pinned(size_t(bytes), node);
-    if (!*out) HQ_CHECK_CUDA(cudaHostAlloc(out, bytes, cudaHostAllocDefault));
+    HQ_CHECK_CUDA(cudaHostAlloc(out, bytes, cudaHostAllocDefault));
     HQ_API_END
 }
 
 hq_status hq_host_free(void* p) {
     HQ_API_BEGIN
-    if (!p) return HQ_OK;
-    size_t mapped = 0;
-    {
-        std::lock_guard<std::mutex> lk(g_host_mu);
-        auto it = g_host_mapped.find(p);
-        if (it != g_host_mapped.end()) {
-            mapped = it->second;
-            g_host_mapped.erase(it);
-        }
-    }
-    if (mapped) {
-        HQ_CHECK_CUDA(cudaHostUnregister(p));
-        munmap(p, mapped);
-    } else {
-        HQ_CHECK_CUDA(cudaFreeHost(p));
-    }
+    if (p) HQ_CHECK_CUDA(cudaFreeHost(p));
     HQ_API_END
 }
 

@@ -82,9 +82,7 @@ hq_status hq_device_info(int32_t* sm_count, uint64_t* hbm_bytes, int32_t* smem_p
 hq_status hq_set_hbm_budget(uint64_t bytes);
 hq_status hq_hbm_in_use(uint64_t* bytes);
 
-/* Page-locked host buffers for fast state transfers.  Buffers of 64 MiB and
- * more are placed on the GPU's own NUMA node (so transfers do not cross a
- * CPU-CPU link) and pinned in place; smaller ones come from cudaHostAlloc. */
+/* Page-locked host buffers for fast state transfers (cudaHostAlloc). */
 hq_status hq_host_alloc(uint64_t bytes, void** out);
 hq_status hq_host_free(void* p);
 

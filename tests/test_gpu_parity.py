@@ -135,9 +135,8 @@ def test_async_readback_orders_with_later_writes(hq, oracle):
 
 
 def test_large_pinned_buffer_readback(hq):
-    """Pinned buffers of 64 MiB and more are mapped on the GPU's NUMA node and
-    registered in place; synchronous and asynchronous readbacks into one match
-    a readback into ordinary memory."""
+    """Synchronous and asynchronous readbacks into a large pinned buffer match a
+    readback into ordinary memory."""
     n = 24
     s = hq.State(n, zero=False)
     s.load(W.random_state(3, n))
