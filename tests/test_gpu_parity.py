@@ -194,6 +194,46 @@ def test_oshm_every_gate_type_in_and_out_of_tile(hq, oracle, t):
     check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
 
 
+def every_placement(n, seed):
+    """Every gate type at every target and every control position (CCX with a
+    rotating second control), parameters seeded."""
+    rng = W.SplitMix64(seed)
+    desc = []
+    for t in ALL_TYPES:
+        for tq in range(n):
+            params = tuple(rng.uniform() * W.TWO_PI for _ in range(NPARAMS.get(t, 0)))
+            if t == W.CCX:
+                for c in range(n):
+                    c2 = (c + 1 + tq) % n
+                    if c != tq and c2 not in (tq, c):
+                        desc.append((t, tq, c, c2, ()))
+            elif t <= W.CRZ:
+                for c in range(n):
+                    if c != tq:
+                        desc.append((t, tq, c, -1, params))
+            else:
+                desc.append((t, tq, -1, -1, params))
+    return desc
+
+
+@pytest.mark.parametrize("tile,specialize", [(10, 2), (12, 2), (10, 0)])
+def test_every_gate_at_every_position_compiled(hq, oracle, tile, specialize):
+    """Exhaustive placements on 12 qubits through the compiled OShareMem path:
+    targets and controls inside and outside the tile, on the vector lane, in a
+    warp and across warps (12-qubit tiles run 4 warps), generated kernels and
+    the interpreter."""
+    n = 12
+    desc = every_placement(n, 1234)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile("oshm", tile_qubits=tile, specialize=specialize)
+    psi = W.random_state(77, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    c.run_on(s)
+    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_oshm_scattered_tile(hq, oracle, seed):
     """Tile = qubit 0 + 12 random qubits of 18; gates of every type with
