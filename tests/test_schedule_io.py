@@ -135,3 +135,27 @@ def test_size_query_and_small_buffer():
                                   C.byref(size))
     assert rc == HQ_ERR_INVALID
     assert size.value == len(hq.plan_schedule(n, gates))
+
+
+def test_mutated_bytes_never_crash():
+    """Random field damage past the checksum (bytes resealed) is either a valid
+    schedule or a clean HQ_ERR_* error -- the loader never reads out of bounds."""
+    n = 14
+    gates = W.to_gates(W.grid_random(8, 2, 7, 6))
+    body = hq.plan_schedule(n, gates)[:-8]
+    rng = W.SplitMix64(2024)
+    ok = refused = 0
+    for _ in range(400):
+        b = bytearray(body)
+        for _ in range(1 + rng.below(3)):
+            pos = rng.below(len(b))
+            b[pos] = rng.below(256)
+        if rng.below(4) == 0:  # truncate or extend as well
+            b = b[:rng.below(len(b))] if rng.below(2) else b + bytes(rng.below(64))
+        try:
+            hq.inspect_schedule(reseal(bytes(b)))
+            ok += 1
+        except hq.HQError as e:
+            assert e.code in (HQ_ERR_INVALID, HQ_ERR_UNSUPPORTED)
+            refused += 1
+    assert refused > 0 and ok + refused == 400
