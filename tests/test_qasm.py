@@ -126,3 +126,27 @@ def test_parsed_qft_runs(hq, oracle):
     ref = np.fft.ifft(psi.astype(np.complex128)) * np.sqrt(1 << n)
     cmp = oracle.compare(ref, s.store())
     assert cmp["max_abs_err"] <= 1e-5 and cmp["one_minus_fidelity"] <= 1e-6, cmp
+
+
+def test_mutated_text_never_crashes():
+    """Damaged QASM (random characters replaced, cut short, lines repeated) is
+    either parsed or refused with an error -- the parser never misbehaves."""
+    rng = W.SplitMix64(99)
+    alphabet = "qc[](),;.*/+-0123456789 piuxyzhtsdgcrOPENQASM\n"
+    ok = refused = 0
+    for _ in range(300):
+        t = list(TEXT)
+        for _ in range(1 + rng.below(6)):
+            t[rng.below(len(t))] = alphabet[rng.below(len(alphabet))]
+        text = "".join(t)
+        if rng.below(3) == 0:
+            text = text[:rng.below(len(text))]
+        try:
+            n, gates = hq.parse_qasm(text)
+            assert 0 < n <= 36
+            for g in gates:
+                assert 0 <= g.g.target < n
+            ok += 1
+        except hq.HQError:
+            refused += 1
+    assert ok + refused == 300 and refused > 0
