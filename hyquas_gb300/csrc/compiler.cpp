@@ -270,8 +270,38 @@ void absorb_small_groups(Partition& part, const std::vector<hq_gate>& gates,
     }
 }
 
+namespace {
+Partition partition_greedy(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
+                           const CompileConfig& cfg);
+}  // namespace
+
+// The greedy grouping in gate order, and (GB300 widths) the same greedy over
+// the gates in reverse order with its groups played back in reverse (the
+// dependencies of a reversed circuit are the reversed ones, so the played-back
+// groups are a valid schedule); the one with fewer passes is kept, the
+// forward one on a tie.  The reference's grouping is only the forward greedy.
 Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
                     const CompileConfig& cfg) {
+    Partition fwd = partition_greedy(n, gates, pos0, cfg);
+    if (cfg.reference || gates.size() < 2) return fwd;
+    const int N = (int)gates.size();
+    std::vector<hq_gate> rev(gates.rbegin(), gates.rend());
+    Partition back = partition_greedy(n, rev, pos0, cfg);
+    if (back.groups.size() >= fwd.groups.size()) return fwd;
+    Partition out;
+    for (auto it = back.groups.rbegin(); it != back.groups.rend(); ++it) {
+        GroupPlan gp = *it;
+        for (int& x : gp.gates) x = N - 1 - x;
+        std::sort(gp.gates.begin(), gp.gates.end());
+        out.groups.push_back(std::move(gp));
+    }
+    out.final_pos = fwd.final_pos;  // layouts stay the identity outside reference grouping
+    return out;
+}
+
+namespace {
+Partition partition_greedy(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
+                           const CompileConfig& cfg) {
     Partition out;
     GroupingInput in;
     in.n = n;
@@ -371,6 +401,7 @@ Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<
     if (!cfg.reference) absorb_small_groups(out, gates, in.diag, n, 16);
     return out;
 }
+}  // namespace
 
 // ---- OShareMem lowering ---------------------------------------------------------
 
