@@ -92,3 +92,51 @@ def test_group_order_respects_dependencies():
         for j in range(i + 1, len(desc)):
             if qubits(desc[i]) & qubits(desc[j]):
                 assert pos[i] < pos[j], (i, j)
+
+
+DIAGONAL = {W.CZ, W.CU1, W.CRZ, W.U1, W.Z, W.S, W.SDG, W.T, W.TDG, W.RZ}
+
+
+def families():
+    out = []
+    for s in range(3):
+        out.append((f"grid30_{s}", 30, W.grid_random(2 + s, 5, 6, 20)))
+        out.append((f"grid28_{s}", 28, W.grid_random(10 + s, 4, 7, 24)))
+        out.append((f"ryrz26_{s}", 26, W.ry_rz_cz(W.SplitMix64(20 + s), 26, 30)))
+        out.append((f"u3cnot24_{s}", 24, W.plain_u3_cnot(30 + s, 24, 12)))
+    out.append(("qft24", 24, [g for g in W.qft(24) if g[0] != W.SWAP]))
+    return out
+
+
+@pytest.mark.parametrize("backend", [hq.BACKEND_OSHM, hq.BACKEND_HYBRID, hq.BACKEND_TRANSMM])
+def test_schedules_are_valid_in_either_direction(backend):
+    """The partitioner may keep the greedy over the reversed circuit; whichever
+    it keeps, every gate runs once, every pair of gates that share a qubit and do
+    not commute keeps its program order, and each OShareMem group's
+    non-diagonal targets lie in its related qubits."""
+    qubits = lambda d: {d[1]} | {q for q in (d[2], d[3]) if q >= 0}
+    for name, n, desc in families():
+        groups = plan(n, desc, backend, reference=False)
+        pos, k = {}, 0
+        for g in groups:
+            for x in g["gates"]:
+                assert x not in pos, (name, x)
+                pos[x] = k
+                k += 1
+            if g["backend"] == hq.BACKEND_OSHM:
+                for x in g["gates"]:
+                    if desc[x][0] not in DIAGONAL:
+                        assert (g["related"] >> desc[x][1]) & 1, (name, x)
+        assert sorted(pos) == list(range(len(desc))), name
+        by_qubit = {}
+        for i, d in enumerate(desc):
+            for q in qubits(d):
+                by_qubit.setdefault(q, []).append(i)
+        for q, idx in by_qubit.items():
+            last_any = last_nondiag = -1  # latest schedule positions so far on q
+            for b in idx:
+                diag = desc[b][0] in DIAGONAL
+                assert pos[b] > (last_nondiag if diag else last_any), (name, q, b)
+                last_any = max(last_any, pos[b])
+                if not diag:
+                    last_nondiag = max(last_nondiag, pos[b])
