@@ -7,8 +7,9 @@
 // gathers, every op with its matrix as literals, register controls resolved
 // per amplitude at generation time -- and compiles it with NVRTC for sm_103a
 // (loaded through the runtime's library API).  The tile framework (persistent
-// CTAs, double-buffered cp.async staging, swizzled shared memory, f32x2 math)
-// is the interpreter's; only the op stream becomes straight-line code.
+// CTAs, cp.async staging, swizzled shared memory, f32x2 math) is the
+// interpreter's; only the op stream becomes straight-line code, with the
+// vectors' scales and signs tracked at generation time.
 //
 // NVRTC is opened at run time; when it is missing, compile falls back to the
 // interpreter kernel (both are GPU paths).
@@ -148,9 +149,10 @@ struct Gen {
     // Per-slot signed scales within a phase: register vector j (and its
     // imaginary partner) holds sigma_j = (neg_j ? -1 : 1) sqrt(2)^e_j times its
     // true amplitudes.  Exact 45-degree phases (T, T^dagger) then cost one add
-    // per component, the slot's scale growing by sqrt 2, and the adds of H,
-    // sqrt(X) and sqrt(Y) absorb a scale ratio as one FMA; the phase's closing
-    // multiply divides every slot by its scale.
+    // per component, the slot's scale growing by sqrt 2; a sign flip on a
+    // register qubit (Z, CZ) only flips the slot's sign; the adds of H, sqrt(X)
+    // and sqrt(Y) absorb a scale ratio as one FMA; the phase's closing multiply
+    // divides every slot by its scale.
     std::vector<int> se;
     std::vector<char> sn;
     void reset_scales() {
