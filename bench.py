@@ -333,7 +333,8 @@ def run_ours(args, dist: Dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
         "config": {"workload": workload, "backend": args.backend, "passes": len(sched),
                    "oshm_groups": groups_oshm, "transmm_groups": len(sched) - groups_oshm,
-                   "reference_groups_tile10": 17, "compile_ms": compile_ms,
+                   "reference_groups_tile10": len(hq.plan_groups(n, gates, reference_grouping=True)),
+                   "compile_ms": compile_ms,
                    "l2": f"state ({8 << n >> 20} MiB) larger than L2; no flush",
                    "parallelism": f"replicas x{dist.ws}"},
         "roofline": roofline,

@@ -328,6 +328,25 @@ def _compile_options(backend="oshm", tile_qubits=0, coalesce=0, mm_qubits=0, pre
     return o
 
 
+def plan_groups(num_qubits: int, gates, **options) -> list[dict]:
+    """Host only: the gate groups compile would make (hq_plan_groups), each as
+    {backend, gates (indices), width, related, phases}."""
+    arr = gate_array(gates)
+    o = _compile_options(**options)
+    k = max(1, len(gates))
+    ng = C.c_int32()
+    b, g, w = (C.c_int32 * k)(), (C.c_int32 * k)(), (C.c_int32 * k)()
+    rel, ph, order = (C.c_uint64 * k)(), (C.c_int32 * k)(), (C.c_int32 * k)()
+    check(lib.hq_plan_groups(num_qubits, arr, len(gates), C.byref(o), C.byref(ng), b, g, w, rel, ph,
+                             order))
+    out, off = [], 0
+    for i in range(ng.value):
+        out.append({"backend": b[i], "gates": list(order[off:off + g[i]]), "width": w[i],
+                    "related": rel[i], "phases": ph[i]})
+        off += g[i]
+    return out
+
+
 def plan_schedule(num_qubits: int, gates, **options) -> bytes:
     """Host only: the schedule bytes compile would make for these gates (the
     reference's Schedule::serialize, src/schedule.cpp:156-325)."""

@@ -140,3 +140,14 @@ def test_schedules_are_valid_in_either_direction(backend):
                 last_any = max(last_any, pos[b])
                 if not diag:
                     last_nondiag = max(last_nondiag, pos[b])
+
+
+def test_package_plan_groups_matches_the_abi():
+    desc = W.grid_random(2, 5, 6, 20)
+    gates = W.to_gates(desc)
+    for ref in (True, False):
+        a = hq.plan_groups(30, gates, reference_grouping=ref)
+        b = plan(30, desc, hq.BACKEND_OSHM, reference=ref)
+        assert [(g["backend"], g["gates"], g["related"]) for g in a] == \
+               [(g["backend"], g["gates"], g["related"]) for g in b]
+    assert len(hq.plan_groups(30, gates, reference_grouping=True)) == 17
