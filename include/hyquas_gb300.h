@@ -80,10 +80,12 @@ hq_status hq_device_info(int32_t* sm_count, uint64_t* hbm_bytes, int32_t* smem_p
 /* Set the HBM budget (bytes) that state allocation is admitted against;
  * 0 = no budget.  No reference counterpart (the reference has no admission). */
 hq_status hq_set_hbm_budget(uint64_t bytes);
+/* Device bytes the library holds (states, programs, scratch). */
 hq_status hq_hbm_in_use(uint64_t* bytes);
 
 /* Page-locked host buffers for fast state transfers (cudaHostAlloc). */
 hq_status hq_host_alloc(uint64_t bytes, void** out);
+/* Frees a buffer from hq_host_alloc. */
 hq_status hq_host_free(void* p);
 
 /* ---- gates (src/gate.cpp:9-342, the Gate::* factories) ---------------- */
@@ -133,6 +135,7 @@ hq_status hq_state_wait(hq_state s);
 hq_status hq_state_amps(hq_state s, const uint64_t* logical_idx, int64_t count, float* out);
 /* Current logical->physical qubit map (State::pos, src/schedule.h:15-34). */
 hq_status hq_state_layout(hq_state s, int32_t* pos);
+/* Circuit::numQubits for a state (src/circuit.h:20-46). */
 hq_status hq_state_num_qubits(hq_state s, int32_t* n);
 /* Device pointer of the amplitudes (physical order); for zero-copy users. */
 hq_status hq_state_device_ptr(hq_state s, void** dev_ptr);
@@ -203,12 +206,16 @@ typedef struct hq_compile_options {
                               when NVRTC is present, else interpreter (default) */
 } hq_compile_options;
 
+/* OShareMem backend, autotuned widths, split BF16, generated kernels when
+ * available (the reference's default build: -DBACKEND=group). */
 hq_status hq_compile_options_default(hq_compile_options* opt);
 
+/* Circuit(int numQubits), src/circuit.h:20-46; destroy frees its device program. */
 hq_status hq_circuit_create(int32_t num_qubits, hq_circuit* out);
 hq_status hq_circuit_destroy(hq_circuit c);
 /* Circuit::addGate, src/circuit.h:28-30. */
 hq_status hq_circuit_add_gates(hq_circuit c, const hq_gate* gates, int32_t num_gates);
+/* Gates added so far (the reference's Circuit::gates.size()). */
 hq_status hq_circuit_num_gates(hq_circuit c, int32_t* num_gates);
 /* Circuit::compile, src/circuit.cpp:177-210 (Compiler::run, src/compiler.cpp:70-165). */
 hq_status hq_circuit_compile(hq_circuit c, const hq_compile_options* opt);
@@ -272,6 +279,8 @@ hq_status hq_circuit_enqueue(hq_circuit c, hq_state s);
  * path circuits are captured too: one kernel node per gate, no host launch per
  * gate on replay. */
 hq_status hq_circuit_capture_graph(hq_circuit c, hq_state s);
+/* Wait for all work queued on the library stream (cudaDeviceSynchronize in the
+ * reference's timed region, src/circuit.cpp:16-71). */
 hq_status hq_synchronize(void);
 
 /* ---- cost model and autotuner (replace the reference's V100/A100 parameter
@@ -289,7 +298,9 @@ typedef struct hq_cost_params {
     double mm_fp32;         /* 6-qubit TransMM pass, FP32 SIMT (x 2^(m-6) beyond 6) */
     double launch;          /* seconds per launch */
 } hq_cost_params;
+/* The cost model in use (defaults fitted on GB300, or hq_autotune's). */
 hq_status hq_cost_params_get(hq_cost_params* out);
+/* Install cost-model constants (e.g. ones measured earlier by hq_autotune). */
 hq_status hq_cost_params_set(const hq_cost_params* p);
 /* Measure the parameters on this GPU with a num_qubits-qubit scratch state
  * (0 = 26; a few seconds, including kernel generation) and install them;
@@ -301,6 +312,7 @@ hq_status hq_autotune(int32_t num_qubits, hq_cost_params* out);
  * Many circuits of uneven qubit counts run in ONE persistent launch that pulls
  * (circuit, gate group, tile range) items from a device work queue. */
 typedef struct hq_batch_s* hq_batch;
+/* An empty batch; destroy frees its device program (not the states). */
 hq_status hq_batch_create(hq_batch* out);
 hq_status hq_batch_destroy(hq_batch b);
 /* Add circuit c (its gates are copied; it need not be compiled) to run on
@@ -363,9 +375,12 @@ hq_status hq_server_options_default(hq_server_options* opt);
  * state bytes against the budget); the checks hq_server_submit makes. */
 hq_status hq_server_check(const hq_server_options* opt, int32_t num_qubits, const hq_gate* gates,
                           int32_t num_gates);
+/* Starts the planner threads and the engine thread. */
 hq_status hq_server_create(const hq_server_options* opt, hq_server* out);
 /* Stops the engine (the step in flight completes) and frees every state. */
 hq_status hq_server_destroy(hq_server sv);
+/* Queue a circuit (returns at once with its id); planning runs on the
+ * planner threads, admission by state bytes against the HBM budget. */
 hq_status hq_server_submit(hq_server sv, int32_t num_qubits, const hq_gate* gates,
                            int32_t num_gates, int64_t* id);
 /* Wait up to timeout_s for request id to finish; *status = HQ_REQ_*. */
@@ -388,6 +403,8 @@ hq_status hq_server_steps(hq_server sv, int64_t id, int64_t* first_step, int64_t
 hq_status hq_server_plan_cache(hq_server sv, int64_t* hits, int64_t* entries);
 /* Frees the request's state (finished requests only). */
 hq_status hq_server_release(hq_server sv, int64_t id);
+/* Engine counters: steps run, work items, finished requests, resident and
+ * peak state bytes. */
 hq_status hq_server_stats(hq_server sv, int64_t* steps, int64_t* items, int64_t* finished,
                           uint64_t* resident_bytes, uint64_t* peak_resident_bytes);
 
