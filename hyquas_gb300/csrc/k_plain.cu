@@ -342,6 +342,18 @@ extern "C" hq_status hq_marginals_noalloc(const void* d_state, int32_t num_qubit
                    num_qubits, kNoAllocMaxQubits, (unsigned long long)kNoAllocDoubles);
         HQ_REQUIRE(((uintptr_t)d_state & 15) == 0 && ((uintptr_t)d_out & 7) == 0, HQ_ERR_INVALID,
                    "d_state must be 16-byte and d_out 8-byte aligned");
+        {
+            // The scratch address is per device: a state on another device
+            // (or in another context) would pair with the wrong array.
+            int dev = -1;
+            HQ_CHECK_CUDA(cudaGetDevice(&dev));
+            cudaPointerAttributes attr{};
+            HQ_CHECK_CUDA(cudaPointerGetAttributes(&attr, d_state));
+            HQ_REQUIRE(attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged,
+                       HQ_ERR_INVALID, "d_state is not device memory");
+            HQ_REQUIRE(attr.device == dev, HQ_ERR_INVALID,
+                       "d_state lives on device %d but device %d is current", attr.device, dev);
+        }
         double* scratch = noalloc_scratch_current_device();
         cudaStream_t st = (cudaStream_t)stream;
         const int n = num_qubits;

@@ -84,7 +84,9 @@ __global__ void k_draw(const float2* __restrict__ a, uint64_t namps, const doubl
     const double total = cdf[nb - 1];
     const double u = double(mix64(seed + 0x9e3779b97f4a7c15ull * uint64_t(shot + 1)) >> 11) *
                      (1.0 / 9007199254740992.0);
-    const double target = u * total;
+    // rounded product (never fused into the subtraction below), so the FP64
+    // steps of a draw are fixed and can be restated exactly on the host
+    const double target = __dmul_rn(u, total);
     // first block whose cumulative probability exceeds the target
     uint64_t lo = 0, hi = nb - 1;
     while (lo < hi) {

@@ -167,7 +167,10 @@ hq_status hq_state_sample(hq_state s, int32_t shots, uint64_t seed, uint64_t* ou
  * that loads it until exit), so num_qubits is limited to 26; larger sizes
  * return HQ_ERR_INVALID.  The first call on a device looks up the array's
  * address with that device current: make it before any stream capture.
- * All calls share the array: calls that overlap on the GPU race. */
+ * All calls share the array: calls that overlap on the GPU race.
+ * d_state, d_out and stream must belong to the current device and its
+ * primary context (the one the CUDA runtime uses); a state on another device
+ * returns HQ_ERR_INVALID. */
 hq_status hq_marginals_noalloc(const void* d_state, int32_t num_qubits, double* d_out,
                                void* stream);
 /* ---- plain path (BACKEND=serial): one launch per gate ------------------- */

@@ -40,6 +40,16 @@ int oracle_gate_matrix(int type, const double* params, double mat[8]);
 int oracle_apply_f64(int n, double* state, const oracle_gate* gates, int ngates, int nthreads);
 int oracle_apply_f32(int n, float* state, const oracle_gate* gates, int ngates, int nthreads);
 
+/* Same result as oracle_apply_f64, bit for bit: consecutive gates whose
+ * qubits fit in `width` (1..20) qubits run on cache-sized blocks of the state. */
+int oracle_apply_f64_blocked(int n, double* state, const oracle_gate* gates, int ngates,
+                             int nthreads, int width);
+
+/* out = {max |ref - got|, Re <ref|got>, Im <ref|got>, <ref|ref>, <got|got>}
+ * over `count` amplitudes of an FP64 reference and a complex64 result. */
+void oracle_compare_c64(int64_t count, const double* ref, const float* got, int nthreads,
+                        double* out);
+
 /* |0..0> */
 void oracle_init_zero_f64(int n, double* state);
 void oracle_init_zero_f32(int n, float* state);

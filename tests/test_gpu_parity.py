@@ -468,6 +468,23 @@ def test_grid_circuit_small_vs_oracle(hq, oracle, rows, cols):
     check(oracle, oracle.run_f64(n, desc), s.store())
 
 
+@pytest.mark.parametrize("rows,cols", [(4, 6), (2, 13)])
+def test_grid_circuit_24_26_vs_oracle(hq, oracle, rows, cols):
+    """The headline circuit family at 24 and 26 qubits (20 cycles, the
+    generated OShareMem kernels at the default 13-qubit tiles) against the
+    FP64 gate-by-gate oracle on the whole state."""
+    n = rows * cols
+    desc = W.grid_random(2, rows, cols, 20)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile("oshm")
+    s = hq.State(n)
+    c.run_on(s)
+    got = s.store()
+    s.free()
+    check(oracle, oracle.run_f64(n, desc), got)
+
+
 def inverse(desc):
     inv = {W.T: W.TDG, W.TDG: W.T, W.S: W.SDG, W.SDG: W.S}
     out = []

@@ -124,7 +124,8 @@ def test_sampler_matches_oracle(hq, oracle, n):
     amps = s.store()
     got = s.sample(3000, seed=1234 + n)
     ref = oracle.sample(amps, 3000, 1234 + n)
-    assert np.mean(got == ref) >= 0.995
+    # the oracle adds the FP64 probabilities in the sampler's order: every index agrees
+    assert np.array_equal(got, ref), np.nonzero(got != ref)[0][:10]
     # outcome frequencies follow |amp|^2
     p = np.abs(amps.astype(np.complex128)) ** 2
     assert np.all(p[got.astype(np.int64)] > 0)

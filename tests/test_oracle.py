@@ -75,3 +75,54 @@ def test_prob_zero_matches_numpy():
         p = O.lib.oracle_prob_zero_f32(n, psi.ctypes.data, q, 2)
         mask = ((np.arange(1 << n) >> q) & 1) == 0
         assert abs(p - np.sum(np.abs(psi[mask].astype(np.complex128)) ** 2)) < 1e-12
+
+
+@pytest.mark.parametrize("n,width", [(12, 5), (18, 14), (19, 9)])
+def test_blocked_application_is_bit_identical(n, width):
+    """The cache-blocked FP64 application runs the same operations on every
+    amplitude as the flat gate-by-gate one: identical bits, every gate type,
+    controls inside and outside a block's qubits."""
+    rng = W.SplitMix64(300 + n)
+    desc = []
+    for _ in range(250):
+        t = rng.below(22)
+        qs = rng.shuffle(list(range(n)))[:3]
+        params = tuple(rng.uniform() * W.TWO_PI for _ in range(3))
+        if t == W.CCX:
+            desc.append((t, qs[2], qs[0], qs[1], ()))
+        elif t <= W.CRZ:
+            desc.append((t, qs[1], qs[0], -1, params[:1]))
+        else:
+            desc.append((t, qs[0], -1, -1, params))
+    psi = W.random_state(9, n).astype(np.complex128)
+    flat = O.apply_f64(n, psi, desc, blocked=False)
+    arr, k = O.gate_structs(desc)
+    blk = psi.copy()
+    assert O.lib.oracle_apply_f64_blocked(n, blk.ctypes.data, arr, k, 4, width) == 0
+    assert np.array_equal(flat, blk)
+
+
+def test_compare_one_pass_matches_numpy():
+    rng = np.random.default_rng(3)
+    ref = (rng.normal(size=4096) + 1j * rng.normal(size=4096)).astype(np.complex128)
+    got = (ref + 1e-4 * rng.normal(size=4096)).astype(np.complex64)
+    fast = O.compare(ref, got)
+    slow = O.compare(ref, got.astype(np.complex128))
+    assert abs(fast["max_abs_err"] - slow["max_abs_err"]) < 1e-12
+    assert abs(fast["one_minus_fidelity"] - slow["one_minus_fidelity"]) < 1e-9
+
+
+def test_sampler_restatement_follows_the_cdf():
+    """The oracle sampler (the sampler's FP64 summation order) lands every
+    shot on an index whose CDF interval holds u * total."""
+    n = 13
+    a = W.random_state(4, n)
+    a[::7] = 0
+    shots = O.sample(a, 500, 77)
+    p = np.abs(a.astype(np.complex128)) ** 2
+    cdf = np.cumsum(p)
+    u = O._mix64_uniforms(77, 500) * cdf[-1]
+    lo = np.concatenate([[0.0], cdf[:-1]])[shots.astype(np.int64)]
+    hi = cdf[shots.astype(np.int64)]
+    assert np.all(p[shots.astype(np.int64)] > 0)
+    assert np.all((u >= lo - 1e-12) & (u < hi + 1e-12))

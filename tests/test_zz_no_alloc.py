@@ -4,8 +4,9 @@ It serves callers that cannot call cudaMalloc -- device memory owned by another
 allocator, or paths that must not take cudaMalloc's implicit synchronisation --
 so it uses a static device scratch array instead of allocating.  Checked
 through the C ABI against the allocating entry point (hq_state_marginals /
-hq_state_norm) on two calls in a row, the second smaller than the first so
-it runs over the first call's leftover scratch contents.  The caller's device
+hq_state_norm) on calls in a row, each smaller than the one before so it
+runs over the earlier calls' leftover scratch contents, down to 1 and 3 qubits
+where one reduction block sees mostly padding.  The caller's device
 buffers here come from torch, standing in for the caller's own allocator."""
 import ctypes as C
 
@@ -35,7 +36,7 @@ def test_noalloc_marginals_match_allocating_entry_point(hq):
 
     f = _entry(hq)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for seed, n in ((1, 26), (2, 19)):
+    for seed, n in ((1, 26), (2, 19), (3, 3), (4, 1)):
         s = hq.State(n, zero=False)
         s.load(W.random_state(seed, n))
         out = torch.full((n + 1,), float("nan"), dtype=torch.float64, device="cuda")
@@ -53,3 +54,25 @@ def test_noalloc_marginals_rejects_sizes_beyond_its_scratch(hq):
     assert rc == -1
     assert b"allocation-free range" in hq.lib.hq_last_error()
     assert f(None, 10, C.c_void_p(256), None) == -1
+
+
+def test_noalloc_marginals_allocate_no_device_memory(hq):
+    """After a first call (which looks up the scratch address), further calls
+    leave the device's free memory unchanged."""
+    import torch
+
+    f = _entry(hq)
+    n = 22
+    s = hq.State(n, zero=False)
+    s.load(W.random_state(5, n))
+    out = torch.empty((n + 1,), dtype=torch.float64, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert f(_dev_ptr(hq, s), n, C.c_void_p(out.data_ptr()), stream) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert f(_dev_ptr(hq, s), n, C.c_void_p(out.data_ptr()), stream) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 >= free0, (free0, free1)
+    s.free()
