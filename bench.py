@@ -185,9 +185,21 @@ def cpu_sample(n: int, desc, budget_s: float, threads: int):
     return t_total / k, k
 
 
+def workloads_module():
+    """hyquas_gb300/workloads.py loaded by path: the generators are plain
+    Python, and importing the package would load the native library, which
+    the CPU arms do not use."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("hq_workloads_cpu",
+                                                  ROOT / "hyquas_gb300" / "workloads.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def run_reference(args, dist: Dist):
     """Reference arm: the CPU gate-by-gate port on all host cores."""
-    from hyquas_gb300 import workloads as W
+    W = workloads_module()
     if dist.rank != 0:
         return
     desc = W.grid_random(2, 5, 6, 20)
@@ -216,6 +228,31 @@ def run_reference(args, dist: Dist):
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_leg(name: str, ref) -> dict:
+    """The reference's own single-GPU run on this GPU, outside the timed region:
+    its schedule and kernels (src/kernelOpt.cu run<128> for OShareMem groups,
+    src/kernelSimple.cu for the plain path), traced from its host code and
+    replayed (oracle/ref_replay.cu).  Its "Time Cost" (src/circuit.cpp:46-52),
+    the device time of the same region, its launches, and its state against the
+    FP64 oracle when `ref` is given."""
+    import oracle as O
+    if not O.ref_gpu_available(name):
+        return {"unavailable": f"no trace or cubins for {name} (built where the reference "
+                               "checkout is present: make -C oracle ref-if-present)"}
+    try:
+        r = O.ref_gpu_run(name, repeats=3, want_state=ref is not None)
+    except Exception as e:  # reported, not fatal: it is a baseline
+        return {"unavailable": str(e)}
+    out = {"time_cost_ms": r["time_cost_ms_best"], "time_cost_ms_mean": r["time_cost_ms_mean"],
+           "device_ms": r["device_ms_best"], "launches": r["launches"], "groups": r["groups"],
+           "backend": r["backend"],
+           "how": "reference host code traced against a recording CUDA runtime, its kernels "
+                  "compiled from its sources for sm_103a, replayed on this GPU (best of 3)"}
+    if ref is not None:
+        out.update({"vs_oracle_" + k: v for k, v in O.compare(ref, r["state"]).items()})
+    return out
 
 
 def run_ours(args, dist: Dist):
@@ -313,6 +350,30 @@ def run_ours(args, dist: Dist):
         for b in pinned:
             b.free()
 
+    # accuracy against the FP64 gate-by-gate oracle (outside the timed region):
+    # one fresh run from |0..0>, the whole state read back
+    accuracy = None
+    ref_gpu = None
+    if not args.no_accuracy:
+        import oracle as O
+        state.init_zero()
+        circ.run_on(state)
+        got = np.empty(1 << n, dtype=np.complex64)
+        state.store(got)
+        ta = time.perf_counter()
+        ref = O.run_f64(n, desc)
+        oracle_s = time.perf_counter() - ta
+        accuracy = O.compare(ref, got)
+        accuracy.update({"against": "FP64 gate-by-gate oracle (reference gate matrices), "
+                                    "whole state", "oracle_s": round(oracle_s, 1),
+                         "oracle_threads": O.NTHREADS})
+        del got
+        if (rows, cols) == (5, 6) and not args.no_reference_gpu:
+            ref_gpu = reference_gpu_leg("grid30_group", ref)
+        del ref
+    elif (rows, cols) == (5, 6) and not args.no_reference_gpu:
+        ref_gpu = reference_gpu_leg("grid30_group", None)
+
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -337,6 +398,8 @@ def run_ours(args, dist: Dist):
                    "compile_ms": compile_ms,
                    "l2": f"state ({8 << n >> 20} MiB) larger than L2; no flush",
                    "parallelism": f"replicas x{dist.ws}"},
+        "accuracy": accuracy,
+        "reference_gpu": ref_gpu,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -388,6 +451,7 @@ def run_plain20(args, dist: Dist):
     ref = O.run_f64(n, desc)
     got = state.store()
     err = O.compare(ref, got)
+    ref_gpu = None if args.no_reference_gpu else reference_gpu_leg("plain20_serial", ref)
     peak, peak_kind = measured_peaks()
     per_gate_s = total_s / args.steps / len(desc)
     achieved = 16.0 * (1 << n) / per_gate_s / 1e9
@@ -430,6 +494,8 @@ def run_plain20(args, dist: Dist):
                      "note": "per-gate passes over an L2-resident 8 MiB state: frac above 1 "
                              "measures L2, not HBM"},
         "cpu_baseline": cpu,
+        "reference_gpu": ref_gpu,
+        "accuracy": err,
         "e2e": {"value": dist.ws * args.steps / dist.max(sum(e2e)), "unit": "circuits/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(8 << n)},
         "gpu_launches": (len(desc) + 1) * args.steps, "clocks": clk})
@@ -710,6 +776,10 @@ def main():
     ap.add_argument("--grid", default="5x6", help="grid RxC of the circuit (5x6 = the 30-qubit "
                     "benchmark; smaller grids are for profiler captures)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the replay of the reference's own GPU run")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the FP64 oracle comparison (grid30: about a minute of CPU)")
     ap.add_argument("--workload", default="grid30",
                     choices=["grid30", "plain20", "qft28", "batch", "serve"])
     ap.add_argument("--qft-qubits", type=int, default=28)
