@@ -267,7 +267,8 @@ def run_ours(args, dist: Dist):
     circ = hq.Circuit(n)
     circ.addGates(gates)
     t0 = time.perf_counter()
-    circ.compile(backend=args.backend)
+    circ.compile(backend=args.backend, specialize=args.specialize, tile_qubits=args.tile_qubits,
+                 coalesce=args.coalesce)
     compile_ms = (time.perf_counter() - t0) * 1000.0
     sched = circ.schedule()
     state = hq.State(n)
@@ -327,7 +328,8 @@ def run_ours(args, dist: Dist):
             ta = time.perf_counter()
             c2 = hq.Circuit(n)
             c2.addGates(gates)
-            c2.compile(backend=args.backend)
+            c2.compile(backend=args.backend, specialize=args.specialize,
+                       tile_qubits=args.tile_qubits, coalesce=args.coalesce)
             h2d = c2.program_bytes()
             tb = time.perf_counter()
             st.init_zero()
@@ -340,12 +342,42 @@ def run_ours(args, dist: Dist):
         for st in states:
             st.wait()
         e2e_s = dist.max(time.perf_counter() - t0)
+        # a new circuit every step (same shape, another seed): the compile
+        # includes generating and compiling its group kernels
+        fresh_steps = max(1, min(args.steps, 5))
+        fresh_parts = []
+        f0 = time.perf_counter()
+        for i in range(fresh_steps):
+            st = states[i % 2]
+            ta = time.perf_counter()
+            c2 = hq.Circuit(n)
+            c2.addGates(W.to_gates(W.grid_random(1000 + 97 * i + dist.rank, rows, cols, 20)))
+            c2.compile(backend=args.backend, specialize=args.specialize,
+                       tile_qubits=args.tile_qubits, coalesce=args.coalesce)
+            tb = time.perf_counter()
+            st.init_zero()
+            c2.run_on(st)
+            tc = time.perf_counter()
+            st.store_async(pinned[i % 2].array)
+            del c2
+            fresh_parts.append([round((tb - ta) * 1e3, 1), round((tc - tb) * 1e3, 1)])
+        for st in states:
+            st.wait()
+        fresh_s = dist.max(time.perf_counter() - f0)
         e2e = {"value": dist.ws * args.steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(8 * (1 << n)),
-               "readback": "asynchronous, two states alternating",
+               "readback": "asynchronous (256 MiB copies), two states alternating",
                "readback_gbs": readback_gbs,
+               "pinned_numa_nodes": [b.numa_nodes() for b in pinned],
                "step_parts_ms": {"compile": [p[0] for p in parts], "init_run": [p[1] for p in parts],
-                                 "queue_release": [p[2] for p in parts]}}
+                                 "queue_release": [p[2] for p in parts]},
+               "fresh_circuit": {"value": dist.ws * fresh_steps / fresh_s, "unit": UNIT,
+                                 "steps": fresh_steps,
+                                 "compile_ms": [p[0] for p in fresh_parts],
+                                 "init_run_ms": [p[1] for p in fresh_parts],
+                                 "what": "a new seeded circuit of the same shape every step: "
+                                         "planning and compiling its group kernels are inside "
+                                         "the step"}}
         states[1].free()
         for b in pinned:
             b.free()
@@ -392,10 +424,14 @@ def run_ours(args, dist: Dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-        "config": {"workload": workload, "backend": args.backend, "passes": len(sched),
+        "config": {"workload": workload, "backend": args.backend, "specialize": args.specialize,
+                   "tile_qubits": args.tile_qubits or 13, "coalesce": args.coalesce or 3,
+                   "passes": len(sched),
                    "oshm_groups": groups_oshm, "transmm_groups": len(sched) - groups_oshm,
                    "reference_groups_tile10": len(hq.plan_groups(n, gates, reference_grouping=True)),
                    "compile_ms": compile_ms,
+                   "group_ms": [round(t / 1000.0, 3) for t in prof],
+                   "group_ms_predicted": [round(t / 1000.0, 3) for t in circ.predict()],
                    "l2": f"state ({8 << n >> 20} MiB) larger than L2; no flush",
                    "parallelism": f"replicas x{dist.ws}"},
         "accuracy": accuracy,
@@ -663,53 +699,153 @@ def run_batch(args, dist: Dist):
         print(json.dumps(line), flush=True)
 
 
+def run_remap(args, dist: Dist):
+    """In-HBM qubit remap (the single-GPU form of the reference's global-qubit
+    exchange, src/executor.cpp:59-179): a step moves 8 physical bits of a
+    resident state in one in-place pass and the next step moves them back."""
+    import hyquas_gb300 as hq
+    from hyquas_gb300 import workloads as W
+    hq.init(dist.local)
+    n = args.remap_qubits
+    s = hq.State(n, zero=False)
+    psi = W.random_state(21, n)
+    s.load(psi)
+    ident = list(range(n))
+    moved = [3, 7, 12, 17, n - 6, n - 4, n - 2, n - 1]  # a cycle over 8 bits
+    fwd = ident.copy()
+    for a, b in zip(moved, moved[1:] + moved[:1]):
+        fwd[a] = b
+    layouts = [fwd, ident]
+    for i in range(args.warmup):
+        s.remap(layouts[i % 2])
+    if args.warmup % 2:
+        s.remap(ident)
+    hq.synchronize()
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    clocks.start()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        s.remap(layouts[i % 2])
+    hq.synchronize()
+    dt = time.perf_counter() - t0
+    clk = clocks.stop()
+    dist.barrier()
+    value, total_s = replica_throughput(dist, args.steps, dt)
+    if args.steps % 2:
+        s.remap(ident)
+    idx = np.array(W.SplitMix64(3).shuffle(range(1 << 16))[:2048], dtype=np.uint64) << np.uint64(n - 16)
+    exact = bool(np.array_equal(s.amps(idx), psi[idx.astype(np.int64)]))
+    # a whole reversal (every bit moves): passes of up to 13 tile bits
+    rev = ident[::-1]
+    t1 = time.perf_counter()
+    s.remap(rev)
+    hq.synchronize()
+    rev_ms = (time.perf_counter() - t1) * 1e3
+    s.remap(ident)
+    peak, peak_kind = measured_peaks()
+    per_step = total_s / args.steps
+    achieved = 16.0 * (1 << n) / per_step / 1e9
+    line = base_line(args, dist, f"{n}q in-HBM remap of 8 qubits (remaps/s)", value, "remaps/s",
+                     per_step * 1e3, True,
+                     f"{n}-qubit complex64 state (8 << {n} bytes, larger than L2): 8 physical bits "
+                     "moved by one in-place pass, then moved back",
+                     {"amplitudes_exact_after_round_trips": exact,
+                      "full_reversal_ms": rev_ms,
+                      "l2": "state larger than L2; no flush"})
+    line.update({"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                              "frac": achieved / peak, "traffic": None,
+                              "kernel": "k_permute_bits (timed with host clock around "
+                                        "synchronised steps)", "peak_source": peak_kind},
+                 "cpu_baseline": None, "e2e": None, "gpu_launches": args.steps, "clocks": clk})
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def serve_once(hq, stream, arrays):
+    """Run `stream` (arrival s, n, gates) through a fresh request loop in real
+    time: submit each request at its arrival, read its result (one amplitude
+    and 16 samples) and release it on completion.  Returns circuits/s over the
+    span from first submission to last completion, p50/p99 latency (ms) and
+    the loop's statistics."""
+    sv = hq.Server()
+    w = sv.submit(12, [])
+    sv.wait(w, 60)
+    sv.release(w)
+    sv.poll()
+    count = len(stream)
+    t0 = time.perf_counter()
+    times = {}
+    i = 0
+    while len(times) < count:
+        now = time.perf_counter() - t0
+        while i < count and stream[i][0] <= now:
+            sv.submit(stream[i][1], arrays[i])
+            i += 1
+        for rid in sv.poll():
+            if sv.wait(rid, 0) == "done":
+                st = sv.state(rid)
+                st.amps([0])
+                st.sample(16, seed=rid)
+            times[rid] = sv.times(rid)
+            sv.release(rid)
+        time.sleep(0.0002)
+    lat = np.array([d - s for (s, a, d) in times.values()]) / 1e3
+    first = min(s for s, a, d in times.values())
+    last = max(d for s, a, d in times.values())
+    out = {"circuits_per_s": count / ((last - first) * 1e-6),
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "steps": sv.stats()["steps"], "peak_resident_gb": sv.stats()["peak_resident_bytes"] / 1e9}
+    sv.close()
+    return out
+
+
+def fifo(stream, service):
+    """One server, first come first served: each request starts at the later
+    of its arrival and the previous request's end and takes its measured
+    service time.  Circuits/s over the span and p50/p99 latency (ms)."""
+    fin, lat = 0.0, []
+    for (t, _, _), sv_t in zip(stream, service):
+        fin = max(fin, t) + sv_t
+        lat.append(fin - t)
+    span = fin - stream[0][0]
+    return {"circuits_per_s": len(stream) / span, "p50_ms": float(np.percentile(lat, 50)) * 1e3,
+            "p99_ms": float(np.percentile(lat, 99)) * 1e3}
+
+
 def run_serve(args, dist: Dist):
-    """Poisson streams of circuits through the request loop."""
+    """Poisson streams of circuits through the request loop, against the
+    reference's plain gate-by-gate path run one request at a time."""
     import hyquas_gb300 as hq
     from hyquas_gb300 import workloads as W
     hq.init(dist.local)
     count, nmax = args.serve_count, args.serve_nmax
     rates = [200.0, 1000.0, 5000.0]
-    results = {}
+    results, subset = {}, {}
     base = W.served_stream(5 + dist.rank, count, 1000.0, 12, nmax)
     arrays = [hq.gate_array(W.to_gates(d)) for _, _, d in base]
+    m = min(args.serve_plain_count, count)
     for rate in rates:
         stream = W.served_stream(5 + dist.rank, count, rate, 12, nmax)
-        sv = hq.Server()
-        w = sv.submit(12, [])
-        sv.wait(w, 60)
-        sv.release(w)
-        sv.poll()
-        t0 = time.perf_counter()
-        times = {}
-        i = 0
-        while len(times) < count:
-            now = time.perf_counter() - t0
-            while i < count and stream[i][0] <= now:
-                sv.submit(stream[i][1], arrays[i])
-                i += 1
-            for rid in sv.poll():
-                if sv.wait(rid, 0) == "done":
-                    st = sv.state(rid)
-                    st.amps([0])
-                    st.sample(16, seed=rid)
-                times[rid] = sv.times(rid)
-                sv.release(rid)
-            time.sleep(0.0002)
-        lat = np.array([d - s for (s, a, d) in times.values()]) / 1e3
-        first = min(s for s, a, d in times.values())
-        last = max(d for s, a, d in times.values())
-        results[rate] = {"circuits_per_s": count / ((last - first) * 1e-6),
-                         "p50_ms": float(np.percentile(lat, 50)),
-                         "p99_ms": float(np.percentile(lat, 99)),
-                         "steps": sv.stats()["steps"],
-                         "peak_resident_gb": sv.stats()["peak_resident_bytes"] / 1e9}
-        sv.close()
+        results[rate] = serve_once(hq, stream, arrays)
+        subset[rate] = serve_once(hq, stream[:m], arrays[:m])
         if dist.rank == 0:
-            print(json.dumps({"serve_rate": rate, **results[rate]}), file=sys.stderr, flush=True)
-    # one at a time through the compiled path (same kernels): measured service times
-    serv = []
-    for (t, n, _), arr in zip(base, arrays):
+            print(json.dumps({"serve_rate": rate, **results[rate], "subset": subset[rate]}),
+                  file=sys.stderr, flush=True)
+    # the plain path (src/kernelSimple.cu:335-446), measured: each of the first
+    # m requests alone -- state, one launch per gate, result read -- in turn
+    plain_service = []
+    for (t, n, _), arr in zip(base[:m], arrays[:m]):
+        a = time.perf_counter()
+        s = hq.State(n)
+        s.apply_gates(arr)
+        s.amps([0])
+        s.sample(16, seed=7)
+        plain_service.append(time.perf_counter() - a)
+        s.free()
+    # compiled one request at a time (same kernels as the loop, no batching)
+    comp_service = []
+    for (t, n, _), arr in zip(base[:m], arrays[:m]):
         a = time.perf_counter()
         c = hq.Circuit(n)
         c.addGates(arr)
@@ -717,34 +853,14 @@ def run_serve(args, dist: Dist):
         s = hq.State(n)
         c.run_on(s)
         s.amps([0])
-        serv.append(time.perf_counter() - a)
+        s.sample(16, seed=7)
+        comp_service.append(time.perf_counter() - a)
         s.free()
-    # plain gate-by-gate path: per-gate pass time measured at each qubit count
-    per_gate = {}
-    for n in sorted(set(n for _, n, _ in base)):
-        s = hq.State(n)
-        g = [hq.Gate.RY(q % n, 0.3) for q in range(8)]
-        s.apply_gates(g)
-        hq.synchronize()
-        a = time.perf_counter()
-        s.apply_gates(g)
-        hq.synchronize()
-        per_gate[n] = (time.perf_counter() - a) / len(g)
-        s.free()
-    plain = [len(d) * per_gate[n] for _, n, d in base]
-
-    def fifo(service, rate):
-        stream = W.served_stream(5 + dist.rank, count, rate, 12, nmax)
-        fin, lat = 0.0, []
-        for (t, _, _), sv_t in zip(stream, service):
-            fin = max(fin, t) + sv_t
-            lat.append(fin - t)
-        span = fin - stream[0][0]
-        return {"circuits_per_s": count / span, "p50_ms": float(np.percentile(lat, 50)) * 1e3,
-                "p99_ms": float(np.percentile(lat, 99)) * 1e3}
-
-    one = {r: fifo(serv, r) for r in rates}
-    plain_r = {r: fifo(plain, r) for r in rates}
+    plain_r, comp_r = {}, {}
+    for rate in rates:
+        stream = W.served_stream(5 + dist.rank, count, rate, 12, nmax)[:m]
+        plain_r[rate] = fifo(stream, plain_service)
+        comp_r[rate] = fifo(stream, comp_service)
     head = results[1000.0]
     line = base_line(args, dist, "served circuits/s at 1000/s arrivals (p50/p99 in config)",
                      head["circuits_per_s"], "circuits/s", None, True,
@@ -752,13 +868,18 @@ def run_serve(args, dist: Dist):
                      "RY/RZ+CZ; admission by 2^n x 8 B against 150 GB; results read (amplitude + "
                      "16 samples) and released on completion",
                      {"rates": {str(int(r)): results[r] for r in rates},
-                      "one_at_a_time_compiled": {str(int(r)): one[r] for r in rates},
-                      "one_at_a_time_plain_modelled": {str(int(r)): plain_r[r] for r in rates},
-                      "plain_model": "FIFO of gates x measured per-gate pass time at each n",
-                      "speedup_vs_plain": {str(int(r)): results[r]["circuits_per_s"] /
+                      "subset_requests": m,
+                      "subset_rates": {str(int(r)): subset[r] for r in rates},
+                      "plain_one_at_a_time_measured": {str(int(r)): plain_r[r] for r in rates},
+                      "compiled_one_at_a_time_measured": {str(int(r)): comp_r[r] for r in rates},
+                      "plain_service_s_total": sum(plain_service),
+                      "comparison": f"the first {m} requests of each stream: the request loop "
+                                    "(measured, real time) against each request run alone in "
+                                    "arrival order (measured service times, FIFO queue)",
+                      "speedup_vs_plain": {str(int(r)): subset[r]["circuits_per_s"] /
                                            plain_r[r]["circuits_per_s"] for r in rates},
-                      "speedup_vs_compiled": {str(int(r)): results[r]["circuits_per_s"] /
-                                              one[r]["circuits_per_s"] for r in rates}})
+                      "speedup_vs_compiled": {str(int(r)): subset[r]["circuits_per_s"] /
+                                              comp_r[r]["circuits_per_s"] for r in rates}})
     line.update({"roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None})
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
@@ -776,18 +897,28 @@ def main():
     ap.add_argument("--grid", default="5x6", help="grid RxC of the circuit (5x6 = the 30-qubit "
                     "benchmark; smaller grids are for profiler captures)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--tile-qubits", type=int, default=0,
+                    help="OShareMem tile width (0: the library default, 13)")
+    ap.add_argument("--coalesce", type=int, default=0,
+                    help="low physical qubits kept in every tile (0: the library default)")
+    ap.add_argument("--specialize", type=int, default=2, choices=[0, 1, 2],
+                    help="OShareMem kernels: 0 interpreter, 1 generated, 2 generated where "
+                         "possible (grid30)")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip the replay of the reference's own GPU run")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP64 oracle comparison (grid30: about a minute of CPU)")
     ap.add_argument("--workload", default="grid30",
-                    choices=["grid30", "plain20", "qft28", "batch", "serve"])
+                    choices=["grid30", "plain20", "qft28", "batch", "serve", "remap"])
+    ap.add_argument("--remap-qubits", type=int, default=30)
     ap.add_argument("--qft-qubits", type=int, default=28)
     ap.add_argument("--qft-cases", default="",
                     help="backend:k:precision list for --workload qft28 (default: the full sweep)")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--serve-count", type=int, default=200)
     ap.add_argument("--serve-nmax", type=int, default=32)
+    ap.add_argument("--serve-plain-count", type=int, default=50,
+                    help="requests of each stream also run one at a time on the plain path")
     args = ap.parse_args()
     args.grid = tuple(int(x) for x in args.grid.lower().split("x"))
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -799,7 +930,7 @@ def main():
             run_ours(args, dist)
         else:
             {"plain20": run_plain20, "qft28": run_qft28, "batch": run_batch,
-             "serve": run_serve}[args.workload](args, dist)
+             "serve": run_serve, "remap": run_remap}[args.workload](args, dist)
     finally:
         dist.close()
 

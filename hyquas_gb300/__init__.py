@@ -107,6 +107,7 @@ def _load():
         "hq_circuit_run": [P, P, C.POINTER(D)],
         "hq_circuit_enqueue": [P, P],
         "hq_circuit_profile": [P, P, P],
+        "hq_circuit_predict": [P, P],
         "hq_circuit_program_bytes": [P, C.POINTER(U64)],
         "hq_host_alloc": [U64, C.POINTER(P)],
         "hq_host_free": [P],
@@ -192,6 +193,27 @@ class PinnedBuffer:
         check(lib.hq_host_alloc(nbytes, C.byref(self.ptr)))
         buf = (C.c_char * nbytes).from_address(self.ptr.value)
         self.array = np.frombuffer(buf, dtype=dtype, count=count)
+
+    def numa_nodes(self, samples: int = 16) -> list[int] | None:
+        """NUMA node of `samples` pages spread over the buffer (move_pages with
+        no target nodes only reports where each page is); None where the
+        query is unavailable."""
+        import platform
+        nr = {"x86_64": 279, "aarch64": 239}.get(platform.machine())
+        if nr is None or not self.ptr:
+            return None
+        libc = C.CDLL(None, use_errno=True)
+        page = os.sysconf("SC_PAGE_SIZE")
+        nbytes = self.array.nbytes
+        addrs = [(self.ptr.value + (nbytes - 1) * i // max(1, samples - 1)) // page * page
+                 for i in range(samples)]
+        pages = (C.c_void_p * samples)(*addrs)
+        status = (C.c_int * samples)()
+        rc = libc.syscall(C.c_long(nr), C.c_int(0), C.c_ulong(samples), pages, None, status,
+                          C.c_int(0))
+        if rc != 0:
+            return None
+        return sorted(set(int(x) for x in status))
 
     def free(self):
         if self.ptr:
@@ -639,6 +661,13 @@ class Circuit:
         k = len(self.schedule())
         out = np.zeros(max(1, k), dtype=np.float64)
         check(lib.hq_circuit_profile(self._h, state.handle, out.ctypes.data))
+        return out[:k]
+
+    def predict(self) -> np.ndarray:
+        """The cost model's device time (us) of each group (hq_circuit_predict)."""
+        k = len(self.schedule())
+        out = np.zeros(max(1, k), dtype=np.float64)
+        check(lib.hq_circuit_predict(self._h, out.ctypes.data))
         return out[:k]
 
     def program_bytes(self) -> int:

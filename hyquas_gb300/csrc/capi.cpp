@@ -510,6 +510,14 @@ hq_status hq_circuit_profile(hq_circuit c, hq_state s, double* group_us) {
     HQ_API_END
 }
 
+hq_status hq_circuit_predict(hq_circuit c, double* group_us) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_NONNULL(group_us);
+    circuit_predict(c, group_us);
+    HQ_API_END
+}
+
 hq_status hq_circuit_enqueue(hq_circuit c, hq_state s) {
     HQ_API_BEGIN
     HQ_NONNULL(c);

@@ -156,6 +156,12 @@ void launch_gather(const void* state, const uint64_t* d_phys_idx, int64_t count,
                    void* stream);
 // In-place exchange of two physical bits.
 void launch_bit_swap(void* state, int n, int a, int b, void* stream);
+// In-place permutation of the physical bits in one pass: the amplitude at index
+// x goes to the index whose bit dest_of[b] is bit b of x.  The moved bits and
+// the five lowest must number at most kPermuteMaxTileBits.
+constexpr int kPermuteMaxTileBits = 13;
+int permute_tile_bits(int n, const int* dest_of);
+void launch_permute_bits(void* state, int n, const int* dest_of, void* stream);
 void launch_oshm(const OshmLaunch& p, void* stream);
 int oshm_threads(int k, int r);
 int oshm_reg_bits(int k);

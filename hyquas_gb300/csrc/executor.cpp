@@ -58,15 +58,46 @@ void state_remap(hq_state_s* s, const std::vector<int>& np) {
         seen[np[q]] = 1;
     }
     cudaStream_t st = ctx().stream;
-    for (int q = 0; q < n; q++) {
-        if (s->pos[q] == np[q]) continue;
-        int q2 = -1;
-        for (int x = 0; x < n; x++)
-            if (s->pos[x] == np[q]) q2 = x;
-        launch_bit_swap(s->d, n, s->pos[q], np[q], st);
-        s->pos[q2] = s->pos[q];
-        s->pos[q] = np[q];
+    // the exchanges that bring the layout to np, in order
+    std::vector<std::pair<int, int>> swaps;
+    {
+        std::vector<int> pos = s->pos;
+        for (int q = 0; q < n; q++) {
+            if (pos[q] == np[q]) continue;
+            int q2 = -1;
+            for (int x = 0; x < n; x++)
+                if (pos[x] == np[q]) q2 = x;
+            swaps.push_back({pos[q], np[q]});
+            pos[q2] = pos[q];
+            pos[q] = np[q];
+        }
     }
+    // consecutive exchanges run together as one in-place pass while the bits
+    // they move fit a tile (launch_permute_bits: one read and one write of the
+    // state); a lone exchange runs as one (half the state read and written)
+    size_t i = 0;
+    while (i < swaps.size()) {
+        std::vector<int> dest_of(n);
+        for (int b = 0; b < n; b++) dest_of[b] = b;
+        size_t j = i;
+        while (j < swaps.size()) {
+            std::vector<int> trial = dest_of;
+            for (int b = 0; b < n; b++) {
+                if (trial[b] == swaps[j].first) trial[b] = swaps[j].second;
+                else if (trial[b] == swaps[j].second) trial[b] = swaps[j].first;
+            }
+            if (permute_tile_bits(n, trial.data()) > kPermuteMaxTileBits) break;
+            dest_of.swap(trial);
+            j++;
+        }
+        if (j == i) j = i + 1;  // cannot happen (one exchange moves two bits); kept safe
+        if (j - i == 1)
+            launch_bit_swap(s->d, n, swaps[i].first, swaps[i].second, st);
+        else
+            launch_permute_bits(s->d, n, dest_of.data(), st);
+        i = j;
+    }
+    s->pos = np;
 }
 
 void state_wait_copy(hq_state_s* s) {
@@ -81,7 +112,14 @@ void state_store_async(hq_state_s* s, void* host) {
     if (!s->copy_done) HQ_CHECK_CUDA(cudaEventCreateWithFlags(&s->copy_done, cudaEventDisableTiming));
     HQ_CHECK_CUDA(cudaEventRecord(s->ready, c.stream));
     HQ_CHECK_CUDA(cudaStreamWaitEvent(c.copy_stream, s->ready, 0));
-    HQ_CHECK_CUDA(cudaMemcpyAsync(host, s->d, s->bytes, cudaMemcpyDeviceToHost, c.copy_stream));
+    // 256 MiB per copy: large states go out as a queue of moderate copies
+    // rather than one multi-GiB transfer
+    constexpr size_t kChunk = size_t(256) << 20;
+    for (size_t off = 0; off < s->bytes; off += kChunk) {
+        const size_t len = s->bytes - off < kChunk ? s->bytes - off : kChunk;
+        HQ_CHECK_CUDA(cudaMemcpyAsync((char*)host + off, (const char*)s->d + off, len,
+                                      cudaMemcpyDeviceToHost, c.copy_stream));
+    }
     HQ_CHECK_CUDA(cudaEventRecord(s->copy_done, c.copy_stream));
     s->copy_pending = true;
 }
@@ -421,7 +459,7 @@ void circuit_compile(hq_circuit_s* c, const hq_compile_options& o) {
 void circuit_launch_groups(hq_circuit_s* c, void* state, cudaStream_t st) {
     for (const DeviceGroup& dg : c->dgroups) {
         if (dg.backend == HQ_BACKEND_OSHM && dg.has_jit) {
-            jit_launch(dg.jit, state, uint64_t(1) << (c->n - dg.prog.k), st);
+            jit_launch(dg.jit, state, uint64_t(1) << (c->n - dg.prog.k), ctx().d_error, st);
         } else if (dg.backend == HQ_BACKEND_OSHM) {
             OshmLaunch p = make_oshm_launch(dg.prog, state, c->d_phases + dg.phase_off,
                                             c->d_ops, ctx().d_error);
@@ -459,6 +497,17 @@ double circuit_run(hq_circuit_s* c, hq_state_s* s, bool sync) {
     return double(ms) * 1000.0;
 }
 
+void circuit_predict(const hq_circuit_s* c, double* group_us) {
+    HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
+    for (size_t g = 0; g < c->dgroups.size(); g++) {
+        const DeviceGroup& dg = c->dgroups[g];
+        if (dg.backend == HQ_BACKEND_OSHM)
+            group_us[g] = cost_oshm(c->n, (int)dg.prog.phases.size(), dg.phys_gates, dg.prog.k) * 1e6;
+        else
+            group_us[g] = cost_transmm(c->n, dg.mm_m, dg.mm_precision) * 1e6;
+    }
+}
+
 void circuit_profile(hq_circuit_s* c, hq_state_s* s, double* group_us) {
     HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
     HQ_REQUIRE(s->n == c->n, HQ_ERR_INVALID, "state/circuit size mismatch");
@@ -473,7 +522,7 @@ void circuit_profile(hq_circuit_s* c, hq_state_s* s, double* group_us) {
     for (size_t g = 0; g < ng; g++) {
         const DeviceGroup& dg = c->dgroups[g];
         if (dg.backend == HQ_BACKEND_OSHM && dg.has_jit) {
-            jit_launch(dg.jit, s->d, uint64_t(1) << (c->n - dg.prog.k), st);
+            jit_launch(dg.jit, s->d, uint64_t(1) << (c->n - dg.prog.k), ctx().d_error, st);
         } else if (dg.backend == HQ_BACKEND_OSHM) {
             OshmLaunch p = make_oshm_launch(dg.prog, s->d, c->d_phases + dg.phase_off, c->d_ops,
                                             ctx().d_error);

@@ -107,6 +107,8 @@ void schedule_deserialize(const uint8_t* buf, size_t len, hq_circuit_s* c);
 double circuit_run(hq_circuit_s* c, hq_state_s* s, bool sync);
 void circuit_capture(hq_circuit_s* c, hq_state_s* s);
 void circuit_profile(hq_circuit_s* c, hq_state_s* s, double* group_us);
+// the cost model's device time per group (us) of a compiled circuit
+void circuit_predict(const hq_circuit_s* c, double* group_us);
 void circuit_release(hq_circuit_s* c);
 // Enqueue every group of a compiled circuit on `stream` (no layout handling).
 void circuit_launch_groups(hq_circuit_s* c, void* state, cudaStream_t stream);

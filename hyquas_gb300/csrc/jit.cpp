@@ -102,6 +102,29 @@ DI float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a
 DI unsigned swz(unsigned x) { unsigned f = ((x >> 4) ^ (x >> 7) ^ (x >> 10) ^ (x >> 13)) & 7u; return x ^ (f << 1); }
 DI void cpa16(unsigned s, const void* g) { asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(g) : "memory"); }
 DI float F(unsigned b) { return __int_as_float((int)b); }
+// Bounded wait for phase `par` of the mbarrier at `addr`, decided by the whole
+// group (barrier `gbar`, `cnt` threads): either every thread of the group saw
+// the data land or none goes on.  After about two seconds the group records a
+// timeout in err[0..2] (1, site 40, buffer), waits for its own copies in flight
+// and returns false.
+DI bool wait_full(unsigned addr, unsigned par, unsigned gbar, unsigned cnt, int* err, unsigned b) {
+    unsigned ok = 0;
+    const long long t0 = clock64();
+    // each try suspends the thread for up to ~20 us unless the phase completes
+    // first, so a waiting group issues few instructions
+    for (unsigned it = 0; it < (1u << 20); it++) {
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 20000; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(ok) : "r"(addr), "r"(par) : "memory");
+        if (ok || clock64() - t0 > 4000000000ll) break;
+    }
+    unsigned all;
+    asm volatile("{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.and.pred q, %2, %3, p; selp.u32 %0, 1, 0, q; }"
+                 : "=r"(all) : "r"(ok), "r"(gbar), "r"(cnt) : "memory");
+    if (all) return true;
+    if ((threadIdx.x % cnt) == 0 && atomicCAS(err, 0, 1) == 0) { err[1] = 40; err[2] = (int)b; }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    return false;
+}
 )";
 
 std::string flit(float f) {
@@ -494,19 +517,37 @@ std::string deposit_expr(const char* var, uint32_t nbits, const uint8_t* dst, bo
     return e.str();
 }
 
-// Two shapes of the same kernel.  PAIRED: two CTAs per SM, one tile buffer
-// each, registers capped at 128 so both fit; one CTA's tile load overlaps the
-// other's compute and the SM has 16 warps to hide latency.  SINGLE: one CTA per
-// SM that double-buffers its tiles; used when the paired build would spill.
-enum class Shape { PAIRED, SINGLE };
+// Three shapes of the same kernel.
+//   RING: one CTA per SM with two groups of T threads, each group working on
+//     its own tile (16 warps per SM, registers capped at 128), and three tile
+//     buffers in a ring: tile i of the CTA uses buffer i mod 3 and is computed
+//     by group i mod 2; when a group is done reading tile i's buffer it issues
+//     the cp.async loads of tile i + 3 into it (for the other group).  Their
+//     completion is tracked by cp.async.mbarrier.arrive on mbarrier
+//     (i + 3) mod 6, one per (buffer, consuming group): each mbarrier's
+//     phases are then consumed by one group, in order, so the parity a group
+//     waits for is never that of an older phase still pending.  A group never
+//     waits for a load issued less than a tile's compute earlier, so HBM
+//     traffic overlaps the arithmetic.
+//   PAIRED: two CTAs per SM, one tile buffer each; a CTA loads, computes and
+//     stores in turn (the other CTA computing meanwhile).
+//   SINGLE: one CTA per SM that double-buffers its tiles; used when the
+//     128-register builds would spill.
+enum class Shape { RING, PAIRED, SINGLE };
 
 std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape shape) {
     const bool paired = shape == Shape::PAIRED;
+    const bool ring = shape == Shape::RING;
     const int K = prog.k, R = prog.r, NV = 1 << (R - 1);
     const int T = 1 << (K - R);
     const int PPT = (1 << (K - 1)) / T;
-    threads = T;
-    smem = (paired ? 1 : 2) * (sizeof(float) * 2 << K);
+    const size_t tile_bytes = sizeof(float) * 2 << K;
+    threads = ring ? 2 * T : T;
+    smem = ring ? 3 * tile_bytes + 64 : (paired ? 1 : 2) * tile_bytes;
+    // a group-wide barrier: the whole CTA, or in RING the group's named barrier
+    const std::string SYNC = ring ? "asm volatile(\"bar.sync %0, " + std::to_string(T) +
+                                        ";\" :: \"r\"(gbar) : \"memory\");\n"
+                                  : std::string("__syncthreads();\n");
     const int n = prog.n;
     uint8_t tile_phys[OSHM_MAX_K];
     for (int b = 0, j = 0; b < n; b++)
@@ -516,9 +557,14 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
     g.nv = NV;
     std::ostringstream& o = g.o;
     o << kPrelude;
-    o << "extern \"C\" __global__ void __launch_bounds__(" << T << (paired ? ", 2" : "")
-      << ") hq_oshm_group(float2* __restrict__ state, u64 ntiles) {\n";
-    o << "extern __shared__ float4 smem4[];\nconst unsigned t = threadIdx.x;\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(" << threads
+      << (paired ? ", 2" : ring ? ", 1" : "")
+      << ") hq_oshm_group(float2* __restrict__ state, u64 ntiles, int* __restrict__ err) {\n";
+    if (ring)
+        o << "extern __shared__ float4 smem4[];\nconst unsigned grp = threadIdx.x / " << T
+          << "u, t = threadIdx.x % " << T << "u, gbar = 1u + grp;\n";
+    else
+        o << "extern __shared__ float4 smem4[];\nconst unsigned t = threadIdx.x;\n(void)err;\n";
     // physical offset of local index 2t and its slot
     {
         uint8_t dst[OSHM_MAX_K];
@@ -528,6 +574,13 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
     }
     o << "unsigned sbase; asm(\"{ .reg .u64 p; cvta.to.shared.u64 p, %1; cvt.u32.u64 %0, p; }\" : "
          "\"=r\"(sbase) : \"l\"(smem4));\n";
+    if (ring) {
+        // six mbarriers after the buffers, T arrivals each (one per loading thread)
+        o << "const unsigned mbar = sbase + " << 3 * tile_bytes << "u;\n"
+          << "if (threadIdx.x == 0) for (unsigned b = 0; b < 6; b++) asm volatile("
+             "\"mbarrier.init.shared::cta.b64 [%0], %1;\" :: \"r\"(mbar + 8u * b), \"n\"("
+          << T << ") : \"memory\");\n__syncthreads();\n";
+    }
     // tile base: constant runs of block bits
     o << "auto tile_base = [&](u64 u) -> u64 { return 0ull";
     {
@@ -556,12 +609,16 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
         poff[m] = off;
         pslot[m] = swz_host(local);
     }
-    o << "auto load_tile = [&](u64 u, int b) {\n"
-         "const float2* gsrc = state + tile_base(u) + toff;\n"
+    o << (ring ? "auto load_tile = [&](u64 u, int b, u64 i) {\n" : "auto load_tile = [&](u64 u, int b) {\n")
+      << "const float2* gsrc = state + tile_base(u) + toff;\n"
       << "const unsigned bb = sbase + (unsigned)b * " << ((1u << (K - 1)) * 16u) << "u;\n";
     for (int m = 0; m < PPT; m++)
         o << "cpa16(bb + ((tslot ^ " << pslot[m] << "u) << 3), gsrc + " << hex64(poff[m]) << ");\n";
-    o << "asm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n};\n";
+    if (ring)  // this thread's copies arrive on the tile's mbarrier (tile index mod 6) when they land
+        o << "asm volatile(\"cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\" :: \"r\"(mbar + 8u * "
+             "(unsigned)(i % 6)) : \"memory\");\n};\n";
+    else
+        o << "asm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n};\n";
     // the last phase stores its amplitudes straight from registers to HBM, so
     // the tile buffer is free once that phase has gathered them: a paired CTA
     // then starts loading its next tile under the last phase's arithmetic
@@ -569,7 +626,20 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
     // 16-byte stores of neighbouring threads fill whole 32-byte sectors
     // (otherwise the staged write-back through shared memory coalesces better).
     const bool direct = !prog.phases.empty() && prog.phases.back().g_phys[0] == 1;
-    if (paired && direct) {
+    if (ring) {
+        // tile i of this CTA is tile blockIdx.x + i * gridDim.x: group 0 takes the
+        // even i, group 1 the odd; the first three tiles are loaded up front
+        o << "auto tile_of = [&](u64 i) -> u64 { return (u64)blockIdx.x + i * (u64)gridDim.x; };\n"
+             "if (grp == 0) { if (tile_of(0) < ntiles) load_tile(tile_of(0), 0, 0); "
+             "if (tile_of(2) < ntiles) load_tile(tile_of(2), 2, 2); }\n"
+             "else if (tile_of(1) < ntiles) load_tile(tile_of(1), 1, 1);\n"
+             "for (u64 i = grp; tile_of(i) < ntiles; i += 2) {\n"
+             "const u64 u = tile_of(i);\n"
+             "const unsigned bi = (unsigned)(i % 3);\n"
+             "if (!wait_full(mbar + 8u * (unsigned)(i % 6), (unsigned)((i / 6) & 1), gbar, "
+          << T << "u, err, bi)) return;\n"
+          << "float4* buf = smem4 + bi * " << (1 << (K - 1)) << "u;\n";
+    } else if (paired && direct) {
         o << "u64 u = blockIdx.x;\nif (u < ntiles) load_tile(u, 0);\n";
         o << "for (int it = 0; u < ntiles; it++, u += gridDim.x) {\n"
              "asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\");\n"
@@ -619,8 +689,9 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
                   << "u) >> 1]; r" << j << " = q.x; i" << j << " = q.y; }\n";
         }
         if (lastp) {
-            o << "__syncthreads();\n";  // every amplitude is in registers: the buffer is free
+            o << SYNC;  // every amplitude is in registers: the buffer is free
             if (paired) o << "if (u + gridDim.x < ntiles) load_tile(u + gridDim.x, 0);\n";
+            if (ring) o << "if (tile_of(i + 3) < ntiles) load_tile(tile_of(i + 3), bi, i + 3);\n";
         }
         o << "float2 acc = make_float2(1.f, 0.f);\n(void)acc;\nbool negf = false;\n(void)negf;\n";
         bool uses_acc = false;
@@ -695,7 +766,7 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
             o << "((ulonglong2*)buf)[(sb" << p << " ^ " << c << "u) >> 1] = make_ulonglong2(r" << j
               << ", i" << j << ");\n";
         }
-        o << "__syncthreads();\n}\n";
+        o << SYNC << "}\n";
     }
     if (!direct) {
         // staged write-back; pieces are (re0, re1, im0, im1) after a phase and
@@ -711,9 +782,13 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
                      "*(float4*)(gdst + "
                   << hex64(poff[m]) << ") = w; }\n";
         }
-        o << "__syncthreads();\n";
+        o << SYNC;
+        if (ring) o << "if (tile_of(i + 3) < ntiles) load_tile(tile_of(i + 3), bi, i + 3);\n";
     }
-    o << "}\n}\n";
+    o << "}\n";
+    // a thread leaves with none of its copies in flight
+    if (ring) o << "asm volatile(\"cp.async.wait_all;\" ::: \"memory\");\n";
+    o << "}\n";
     return o.str();
 }
 
@@ -768,13 +843,23 @@ JitKernel compile_source(const std::string& src, int threads, size_t smem) {
 
 bool jit_available() { return nvrtc().ok; }
 
+// The first shape tried: RING unless HQ_OSHM_SHAPE names another ("paired",
+// "single"), a tuning knob for comparing the shapes on a given GPU.
+Shape first_shape() {
+    const char* e = getenv("HQ_OSHM_SHAPE");
+    if (e && !strcmp(e, "paired")) return Shape::PAIRED;
+    if (e && !strcmp(e, "single")) return Shape::SINGLE;
+    return Shape::RING;
+}
+
 std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>& progs) {
     ensure_init();
+    const Shape shape0 = first_shape();
     std::vector<std::string> srcs(progs.size());
     std::vector<int> threads(progs.size());
     std::vector<size_t> smem(progs.size());
     for (size_t i = 0; i < progs.size(); i++)
-        srcs[i] = generate(*progs[i], threads[i], smem[i], Shape::PAIRED);
+        srcs[i] = generate(*progs[i], threads[i], smem[i], shape0);
     std::vector<std::shared_ptr<CacheEntry>> ents(progs.size());
     std::vector<size_t> todo;
     {
@@ -809,10 +894,11 @@ std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>&
                 }
                 try {
                     JitKernel jk = compile_source(srcs[k], threads[k], smem[k]);
-                    // a spill of up to 128 bytes per thread costs less than the second
-                    // CTA gains (measured on the 30-qubit grid); beyond that, one
-                    // double-buffered CTA per SM
-                    if (jk.local_bytes > 128 || jk.blocks_per_sm < 2) {
+                    // a spill of up to 128 bytes per thread costs less than the 16
+                    // warps per SM gain (measured on the 30-qubit grid); beyond that,
+                    // one double-buffered CTA of 8 warps per SM
+                    const int need = shape0 == Shape::PAIRED ? 2 : 1;
+                    if (shape0 != Shape::SINGLE && (jk.local_bytes > 128 || jk.blocks_per_sm < need)) {
                         cudaLibraryUnload(jk.lib);
                         int t2 = 0;
                         size_t s2 = 0;
@@ -841,17 +927,17 @@ std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>&
     return out;
 }
 
-void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, cudaStream_t st) {
+void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, int* err, cudaStream_t st) {
     const uint64_t slots = uint64_t(ctx().sm_count) * k.blocks_per_sm;
     const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
-    void* args[] = {&state, &ntiles};
+    void* args[] = {&state, &ntiles, &err};
     HQ_CHECK_CUDA(cudaLaunchKernel((const void*)k.kern, dim3(grid), dim3(k.threads), args, k.smem, st));
 }
 
 std::string jit_source(const OshmProgram& prog) {
     int t;
     size_t s;
-    return generate(prog, t, s, Shape::PAIRED);
+    return generate(prog, t, s, first_shape());
 }
 
 }  // namespace hq

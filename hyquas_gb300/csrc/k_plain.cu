@@ -1,12 +1,14 @@
 // Plain-path kernels: one launch per gate (the reference's BACKEND=serial,
 // src/kernelSimple.cu:335-446), |0..0> initialisation (src/kernelSimple.cu:9-37),
 // FP64 probability reductions (src/kernelSimple.cu:467-516), amplitude gather
-// (src/kernelSimple.cu:518-522) and the in-HBM qubit exchange used by remaps.
+// (src/kernelSimple.cu:518-522) and the in-HBM qubit remaps (one bit exchange
+// in place, or a whole permutation in one out-of-place pass).
 //
 // All indices are 64-bit (the reference's `int nVec` overflows at n >= 32,
 // src/kernelSimple.cu:338).  Every kernel is HBM-bound.
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <mutex>
 
 #include "common.h"
@@ -278,6 +280,162 @@ void launch_gather(const void* state, const uint64_t* d_idx, int64_t count, void
     const unsigned grid = (unsigned)((count + 255) / 256);
     k_gather<<<grid, 256, 0, (cudaStream_t)stream>>>((const float2*)state, d_idx, count,
                                                      (float2*)d_out);
+    HQ_CHECK_CUDA(cudaGetLastError());
+}
+
+// ---- in-place qubit remap, many bits per pass ---------------------------------------
+//
+// The single-GPU form of the reference's layout change (src/executor.cpp:59-179,
+// a local transpose plus an all-to-all).  One pass applies a permutation of the
+// physical bits that moves at most a tile's worth of them: every amplitude goes
+// from index x to the index whose bit dest_of[b] is bit b of x.  A CTA owns a
+// tile of up to 2^13 amplitudes over the moved bits and the five lowest bits
+// (padded with the next lowest); every other bit stays where it is, so a tile
+// maps onto itself and the pass runs in place.  The tile is read in source
+// order (the five lowest bits contiguous: whole 256-byte runs) into shared
+// memory and written back in destination order (again 256-byte runs); slots
+// are XOR-swizzled so the destination-order reads spread over the banks.
+// One read and one write of each amplitude in the tiles the pass touches.
+struct PermuteParams {
+    // offsets of the local index bits 0-4 / 5-9 / 10-12 in the source and the
+    // destination; write-order index -> local index; slot swizzle of bits 5-12
+    uint64_t src_lo[32], src_mid[32], src_hi[8];
+    uint64_t dst_lo[32], dst_mid[32], dst_hi[8];
+    uint16_t wr_lo[32], wr_mid[32], wr_hi[8];
+    uint16_t swz_mid[32], swz_hi[8];
+    uint8_t rest[64];   // tile-index bit r -> its (unmoved) physical bit
+    int nrest;
+    int tile_bits;
+    uint64_t ntiles;
+};
+
+__global__ void __launch_bounds__(256) k_permute_bits(float2* __restrict__ a,
+                                                      const __grid_constant__ PermuteParams p) {
+    extern __shared__ float2 tile[];
+    const int len = 1 << p.tile_bits;
+    for (uint64_t u = blockIdx.x; u < p.ntiles; u += gridDim.x) {
+        uint64_t base = 0;
+        for (int r = 0; r < p.nrest; r++) base |= ((u >> r) & 1) << p.rest[r];
+        for (int e = threadIdx.x; e < len; e += 256) {
+            const float2 v = a[base + p.src_lo[e & 31] + p.src_mid[(e >> 5) & 31] + p.src_hi[e >> 10]];
+            tile[e ^ p.swz_mid[(e >> 5) & 31] ^ p.swz_hi[e >> 10]] = v;
+        }
+        __syncthreads();
+        for (int w = threadIdx.x; w < len; w += 256) {
+            const int j = p.wr_lo[w & 31] | p.wr_mid[(w >> 5) & 31] | p.wr_hi[w >> 10];
+            a[base + p.dst_lo[j & 31] + p.dst_mid[(j >> 5) & 31] + p.dst_hi[j >> 10]] =
+                tile[j ^ p.swz_mid[(j >> 5) & 31] ^ p.swz_hi[j >> 10]];
+        }
+        __syncthreads();
+    }
+}
+
+int permute_tile_bits(int n, const int* dest_of) {
+    uint64_t t = 0;
+    for (int b = 0; b < n && b < 5; b++) t |= uint64_t(1) << b;
+    for (int b = 0; b < n; b++)
+        if (dest_of[b] != b) t |= uint64_t(1) << b;
+    const int need = popcount64(t), floor_bits = n < 10 ? n : 10;
+    return need > floor_bits ? need : floor_bits;
+}
+
+PermuteParams make_permute_params(int n, const int* dest_of) {
+    PermuteParams p;
+    std::memset(&p, 0, sizeof(p));
+    const int K = permute_tile_bits(n, dest_of), c = n < 5 ? n : 5;
+    HQ_REQUIRE(K <= kPermuteMaxTileBits, HQ_ERR_INVALID, "remap pass moves too many bits");
+    int src_of[64];
+    for (int b = 0; b < n; b++) src_of[dest_of[b]] = b;
+    // local bits: source bits 0..c-1, the moved bits, then the lowest others
+    int loc_src[kPermuteMaxTileBits], nl = 0;
+    uint64_t used = 0;
+    auto take = [&](int b) {
+        if (nl < K && !((used >> b) & 1)) {
+            loc_src[nl++] = b;
+            used |= uint64_t(1) << b;
+        }
+    };
+    for (int b = 0; b < c; b++) take(b);
+    for (int b = 0; b < n; b++)
+        if (dest_of[b] != b) take(b);
+    for (int b = 0; b < n && nl < K; b++) take(b);
+    // every bit outside the tile stays put: the tile maps onto itself
+    for (int b = 0; b < n; b++)
+        HQ_REQUIRE(((used >> b) & 1) || dest_of[b] == b, HQ_ERR_INVALID, "remap tile not closed");
+    auto fill = [&](uint64_t* t, int nent, int first, bool dst) {
+        for (int j = 0; j < nent; j++)
+            for (int b = 0; (1 << b) <= j; b++)
+                if (((j >> b) & 1) && first + b < K)
+                    t[j] |= uint64_t(1) << (dst ? dest_of[loc_src[first + b]] : loc_src[first + b]);
+    };
+    fill(p.src_lo, 32, 0, false);
+    fill(p.src_mid, 32, 5, false);
+    fill(p.src_hi, 8, 10, false);
+    fill(p.dst_lo, 32, 0, true);
+    fill(p.dst_mid, 32, 5, true);
+    fill(p.dst_hi, 8, 10, true);
+    // write order: the local bits that land on destination bits 0..c-1 first
+    int wbit[kPermuteMaxTileBits], nw = 0;
+    uint32_t wused = 0;
+    for (int d = 0; d < c; d++)
+        for (int j = 0; j < K; j++)
+            if (loc_src[j] == src_of[d]) {
+                wbit[nw++] = j;
+                wused |= 1u << j;
+            }
+    for (int j = 0; j < K; j++)
+        if (!((wused >> j) & 1)) wbit[nw++] = j;
+    auto fillw = [&](uint16_t* t, int nent, int first) {
+        for (int w = 0; w < nent; w++)
+            for (int b = 0; (1 << b) <= w; b++)
+                if (((w >> b) & 1) && first + b < K) t[w] |= uint16_t(1) << wbit[first + b];
+    };
+    fillw(p.wr_lo, 32, 0);
+    fillw(p.wr_mid, 32, 5);
+    fillw(p.wr_hi, 8, 10);
+    // swizzle: local bits >= 5 that vary across a destination-order warp fold
+    // onto slot bits 0-4 that do not vary there; the other high bits fold onto
+    // slot bits 0-4 in turn
+    int target[kPermuteMaxTileBits];
+    for (int j = 0; j < K; j++) target[j] = -1;
+    uint32_t taken = 0;
+    for (int b = 0; b < c && b < nw; b++)
+        if (wbit[b] < 5) taken |= 1u << wbit[b];
+    for (int b = 0; b < c && b < nw; b++)
+        if (wbit[b] >= 5)
+            for (int f = 0; f < 5; f++)
+                if (!((taken >> f) & 1)) {
+                    target[wbit[b]] = f;
+                    taken |= 1u << f;
+                    break;
+                }
+    for (int j = 5; j < K; j++)
+        if (target[j] < 0) target[j] = (j - 5) % 5;
+    for (int m = 0; m < 32; m++)
+        for (int b = 0; b < 5; b++)
+            if (((m >> b) & 1) && 5 + b < K) p.swz_mid[m] ^= uint16_t(1) << target[5 + b];
+    for (int m = 0; m < 8; m++)
+        for (int b = 0; b < 3; b++)
+            if (((m >> b) & 1) && 10 + b < K) p.swz_hi[m] ^= uint16_t(1) << target[10 + b];
+    p.tile_bits = K;
+    p.nrest = 0;
+    for (int b = 0; b < n; b++)
+        if (!((used >> b) & 1)) p.rest[p.nrest++] = (uint8_t)b;
+    p.ntiles = uint64_t(1) << (n - K);
+    return p;
+}
+
+void launch_permute_bits(void* state, int n, const int* dest_of, void* stream) {
+    const PermuteParams p = make_permute_params(n, dest_of);
+    const size_t smem = sizeof(float2) << p.tile_bits;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        HQ_CHECK_CUDA(cudaFuncSetAttribute(k_permute_bits, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(sizeof(float2) << kPermuteMaxTileBits)));
+    });
+    const uint64_t cap = uint64_t(ctx().sm_count) * 3;
+    const unsigned grid = (unsigned)(p.ntiles < cap ? p.ntiles : cap);
+    k_permute_bits<<<grid, 256, smem, (cudaStream_t)stream>>>((float2*)state, p);
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 

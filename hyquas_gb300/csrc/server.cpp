@@ -417,7 +417,7 @@ void enqueue_step(hq_server_s* sv, StepBuf& sb, std::vector<Request*>& newly,
         Request* r = jr.first;
         if (r->next == 0) launch_init_zero(r->state->d, r->n, st);
         for (uint32_t g = r->next; g < jr.second; g++)
-            jit_launch(r->jit[g], r->state->d, uint64_t(1) << (r->n - r->progs[g].k), st);
+            jit_launch(r->jit[g], r->state->d, uint64_t(1) << (r->n - r->progs[g].k), sv->d_err, st);
     }
     if (nl) {
         HQ_CHECK_CUDA(cudaMemcpyAsync(sb.d, sb.h, launches_b + items_b, cudaMemcpyHostToDevice, st));

@@ -275,6 +275,11 @@ hq_status hq_circuit_run(hq_circuit c, hq_state s, double* elapsed_us);
  * group_us[g] = device time of group g (num_groups entries).  The reference's
  * MEASURE_STAGE per-group timing, src/executor.cpp:406-458. */
 hq_status hq_circuit_profile(hq_circuit c, hq_state s, double* group_us);
+/* The cost model's device time (us) of each group of a compiled circuit, the
+ * figure the hybrid partitioner compares (hq_cost_params): the counterpart of
+ * the reference's Evaluator::perfPerGate / perfBLAS (src/evaluator.cpp:111-229),
+ * to set beside hq_circuit_profile. */
+hq_status hq_circuit_predict(hq_circuit c, double* group_us);
 /* Enqueue the compiled schedule on the library stream without synchronising. */
 hq_status hq_circuit_enqueue(hq_circuit c, hq_state s);
 /* Capture the compiled schedule for state s into a CUDA graph (replayed by
