@@ -42,6 +42,7 @@ static void init_device(int device) {
     HQ_CHECK_CUDA(cudaMalloc(&c.d_partials, sizeof(double) * c.partials_cap));
     c.pinned_cap = 1 << 16;
     HQ_CHECK_CUDA(cudaMallocHost(&c.h_pinned, sizeof(double) * c.pinned_cap));
+    HQ_CHECK_CUDA(cudaMallocHost(&c.h_error, sizeof(int) * 4));
 }
 
 Context& ctx() {
@@ -104,9 +105,13 @@ void dev_free_ordered(void* p, size_t bytes) {
 
 void check_device_error() {
     Context& c = ctx();
-    int h[4];
-    HQ_CHECK_CUDA(cudaMemcpyAsync(h, c.d_error, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
+    // read into page-locked memory: a pageable destination would make this a
+    // staged, host-synchronous copy behind whatever else the copy engines hold
+    HQ_CHECK_CUDA(cudaMemcpyAsync(c.h_error, c.d_error, sizeof(int) * 4, cudaMemcpyDeviceToHost,
+                                  c.stream));
     HQ_CHECK_CUDA(cudaStreamSynchronize(c.stream));
+    int h[4];
+    for (int i = 0; i < 4; i++) h[i] = c.h_error[i];
     if (h[0] != 0) {
         HQ_CHECK_CUDA(cudaMemsetAsync(c.d_error, 0, sizeof(int) * 4, c.stream));
         HQ_CHECK_CUDA(cudaStreamSynchronize(c.stream));

@@ -282,7 +282,42 @@ void apply_oshm_group(hq_state_s* s, const std::vector<hq_gate>& gates, uint64_t
 
 // ---- circuits ---------------------------------------------------------------------
 
+// Background compiles of released circuits run on (their kernels still land in
+// the process-wide cache for later circuits); finished ones are joined at the
+// next release and the rest when the library unloads.
+struct OrphanJobs {
+    std::mutex mu;
+    std::vector<std::shared_ptr<JitJob>> jobs;
+    void prune() {
+        std::lock_guard<std::mutex> lk(mu);
+        for (size_t i = 0; i < jobs.size();) {
+            bool done;
+            {
+                std::lock_guard<std::mutex> jl(jobs[i]->mu);
+                done = jobs[i]->done;
+            }
+            if (done) {
+                if (jobs[i]->th.joinable()) jobs[i]->th.join();
+                jobs.erase(jobs.begin() + i);
+            } else {
+                i++;
+            }
+        }
+    }
+    ~OrphanJobs() {
+        for (auto& j : jobs)
+            if (j->th.joinable()) j->th.join();
+    }
+};
+OrphanJobs g_orphans;
+
 void circuit_release(hq_circuit_s* c) {
+    if (c->jit_job) {
+        std::lock_guard<std::mutex> lk(g_orphans.mu);
+        g_orphans.jobs.push_back(c->jit_job);
+        c->jit_job.reset();
+    }
+    g_orphans.prune();
     if (c->graph) cudaGraphExecDestroy(c->graph);
     c->graph = nullptr;
     c->graph_state = nullptr;
@@ -322,6 +357,8 @@ CompileConfig config_from_options(const hq_compile_options& o, int n) {
     HQ_REQUIRE(o.mm_precision >= HQ_MM_BF16X3 && o.mm_precision <= HQ_MM_FP32, HQ_ERR_INVALID,
                "unknown TransMM precision %d", o.mm_precision);
     HQ_REQUIRE(cfg.coalesce >= 1, HQ_ERR_INVALID, "coalesce must be >= 1");
+    HQ_REQUIRE(o.specialize >= 0 && o.specialize <= 3, HQ_ERR_INVALID, "specialize %d outside [0,3]",
+               o.specialize);
     cfg.tile = std::min(cfg.tile, n);
     return cfg;
 }
@@ -432,14 +469,41 @@ void circuit_lower(hq_circuit_s* c) {
                 idx.push_back(i);
             }
         if (!progs.empty()) {
+            std::vector<JitKernel> ks;
             try {
                 HQ_REQUIRE(jit_available(), HQ_ERR_UNSUPPORTED, "NVRTC not available");
-                std::vector<JitKernel> ks = jit_compile_groups(progs);
-                for (size_t i = 0; i < idx.size(); i++) {
-                    c->dgroups[idx[i]].jit = ks[i];
-                    c->dgroups[idx[i]].has_jit = true;
+                if (o.specialize != 3 || jit_lookup_cached(progs, ks)) {
+                    if (ks.empty()) ks = jit_compile_groups(progs);
+                    for (size_t i = 0; i < idx.size(); i++) {
+                        c->dgroups[idx[i]].jit = ks[i];
+                        c->dgroups[idx[i]].has_jit = true;
+                    }
+                    c->specialized = true;
+                } else {
+                    // background mode, kernels not compiled yet: compile them on a
+                    // host thread; until they are in, the interpreter runs the groups
+                    auto job = std::make_shared<JitJob>();
+                    for (const OshmProgram* pr : progs) job->progs.push_back(*pr);
+                    job->groups = idx;
+                    std::shared_ptr<JitJob> keep = job;
+                    job->th = std::thread([keep] {
+                        JitJob* jp = keep.get();
+                        std::vector<const OshmProgram*> ps;
+                        for (const OshmProgram& pr : jp->progs) ps.push_back(&pr);
+                        std::vector<JitKernel> out;
+                        std::string err;
+                        try {
+                            out = jit_compile_groups(ps);
+                        } catch (const std::exception& e) {
+                            err = e.what();
+                        }
+                        std::lock_guard<std::mutex> lk(jp->mu);
+                        jp->kernels = out;
+                        jp->err = err;
+                        jp->done = true;
+                    });
+                    c->jit_job = job;
                 }
-                c->specialized = true;
             } catch (const Failure& f) {
                 if (o.specialize == 1) throw;
                 c->specialize_note = f.what();  // auto mode: the interpreter runs these groups
@@ -447,6 +511,32 @@ void circuit_lower(hq_circuit_s* c) {
         }
     }
     c->compiled = true;
+}
+
+void circuit_jit_install(hq_circuit_s* c, bool wait) {
+    std::shared_ptr<JitJob> job = c->jit_job;
+    if (!job) return;
+    {
+        std::lock_guard<std::mutex> lk(job->mu);
+        if (!job->done && !wait) return;
+    }
+    if (job->th.joinable()) job->th.join();
+    c->jit_job.reset();
+    if (!job->err.empty() || job->kernels.size() != job->groups.size()) {
+        c->specialize_note = job->err.empty() ? "specialisation failed" : job->err;
+        return;
+    }
+    for (size_t i = 0; i < job->groups.size(); i++) {
+        c->dgroups[job->groups[i]].jit = job->kernels[i];
+        c->dgroups[job->groups[i]].has_jit = true;
+    }
+    c->specialized = true;
+    // a graph captured meanwhile holds interpreter launches: capture again later
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+        c->graph_state = nullptr;
+    }
 }
 
 void circuit_compile(hq_circuit_s* c, const hq_compile_options& o) {
@@ -479,6 +569,7 @@ double circuit_run(hq_circuit_s* c, hq_state_s* s, bool sync) {
         HQ_CHECK_CUDA(cudaEventCreate(&c->ev0));
         HQ_CHECK_CUDA(cudaEventCreate(&c->ev1));
     }
+    circuit_jit_install(c, false);
     HQ_CHECK_CUDA(cudaEventRecord(c->ev0, st));
     if (c->graph && c->graph_state == s) {
         HQ_CHECK_CUDA(cudaGraphLaunch(c->graph, st));
@@ -510,6 +601,7 @@ void circuit_predict(const hq_circuit_s* c, double* group_us) {
 
 void circuit_profile(hq_circuit_s* c, hq_state_s* s, double* group_us) {
     HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
+    circuit_jit_install(c, false);
     HQ_REQUIRE(s->n == c->n, HQ_ERR_INVALID, "state/circuit size mismatch");
     HQ_REQUIRE(c->opt.backend != HQ_BACKEND_PLAIN && c->n >= 6, HQ_ERR_STATE,
                "plain-path circuits have no groups to profile");
@@ -548,6 +640,7 @@ void circuit_capture(hq_circuit_s* c, hq_state_s* s) {
     HQ_REQUIRE(s->n == c->n, HQ_ERR_INVALID, "state/circuit size mismatch");
     const bool plain = c->opt.backend == HQ_BACKEND_PLAIN || c->n < 6;
     cudaStream_t st = ctx().stream;
+    circuit_jit_install(c, true);  // a graph holds the generated kernels
     // runs start from the canonical layout, so the captured launches (plain
     // gates are lowered through the layout) are the ones every run makes
     state_canonicalize(s);

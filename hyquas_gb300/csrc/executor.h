@@ -5,7 +5,10 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "compiler.h"
@@ -25,6 +28,18 @@ struct hq_state_s {
 };
 
 namespace hq {
+
+// Generated kernels of a circuit being compiled on a host thread while the
+// circuit runs interpreted (compile option specialize = 3, kernels not cached).
+struct JitJob {
+    std::thread th;
+    std::mutex mu;
+    bool done = false;
+    std::vector<OshmProgram> progs;
+    std::vector<size_t> groups;     // dgroups index of each program
+    std::vector<JitKernel> kernels;
+    std::string err;
+};
 
 struct DeviceGroup {
     int backend = HQ_BACKEND_OSHM;
@@ -69,6 +84,7 @@ struct hq_circuit_s {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool specialized = false;           // OShareMem groups run generated kernels
     std::string specialize_note;        // why not, when requested in auto mode
+    std::shared_ptr<hq::JitJob> jit_job;  // generated kernels still compiling
 };
 
 namespace hq {
@@ -110,6 +126,9 @@ void circuit_profile(hq_circuit_s* c, hq_state_s* s, double* group_us);
 // the cost model's device time per group (us) of a compiled circuit
 void circuit_predict(const hq_circuit_s* c, double* group_us);
 void circuit_release(hq_circuit_s* c);
+// Generated kernels compiled on a host thread (specialize = 3): install them
+// once ready (wait = true: wait for them).  Runs call this before launching.
+void circuit_jit_install(hq_circuit_s* c, bool wait);
 // Enqueue every group of a compiled circuit on `stream` (no layout handling).
 void circuit_launch_groups(hq_circuit_s* c, void* state, cudaStream_t stream);
 

@@ -18,6 +18,7 @@
 #include <dlfcn.h>
 
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
 #include <functional>
@@ -792,10 +793,16 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
     return o.str();
 }
 
+// One generated source: compiled once per process.  An entry is pending while
+// its first requester compiles it; later requesters of the same source wait
+// for it rather than compiling it again.
 struct CacheEntry {
     JitKernel k;
     bool ok = false;
+    bool pending = true;
     std::string err;
+    std::mutex m;
+    std::condition_variable cv;
 };
 
 std::mutex g_cache_mu;
@@ -905,26 +912,66 @@ std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>&
                         const std::string src2 = generate(*progs[k], t2, s2, Shape::SINGLE);
                         jk = compile_source(src2, t2, s2);
                     }
+                    std::lock_guard<std::mutex> lk(ents[k]->m);
                     ents[k]->k = jk;
                     ents[k]->ok = true;
                 } catch (const Failure& f) {
+                    std::lock_guard<std::mutex> lk(ents[k]->m);
                     ents[k]->err = f.what();
                 }
+                {
+                    std::lock_guard<std::mutex> lk(ents[k]->m);
+                    ents[k]->pending = false;
+                }
+                ents[k]->cv.notify_all();
             }
         });
     }
     for (auto& th : pool) th.join();
     std::vector<JitKernel> out;
     for (size_t i = 0; i < progs.size(); i++) {
-        if (!ents[i]->ok) {
-            std::lock_guard<std::mutex> lk(g_cache_mu);
-            g_cache.erase(srcs[i]);
-            fail(HQ_ERR_UNSUPPORTED, "%s", ents[i]->err.empty() ? "specialisation failed"
-                                                               : ents[i]->err.c_str());
+        bool ok;
+        std::string err;
+        {
+            // an entry another caller is compiling: wait for it
+            std::unique_lock<std::mutex> lk(ents[i]->m);
+            ents[i]->cv.wait(lk, [&] { return !ents[i]->pending; });
+            ok = ents[i]->ok;
+            err = ents[i]->err;
+        }
+        if (!ok) {
+            {
+                std::lock_guard<std::mutex> lk(g_cache_mu);
+                auto it = g_cache.find(srcs[i]);
+                if (it != g_cache.end() && it->second == ents[i]) g_cache.erase(it);
+            }
+            fail(HQ_ERR_UNSUPPORTED, "%s", err.empty() ? "specialisation failed" : err.c_str());
         }
         out.push_back(ents[i]->k);
     }
     return out;
+}
+
+bool jit_lookup_cached(const std::vector<const OshmProgram*>& progs, std::vector<JitKernel>& out) {
+    const Shape shape0 = first_shape();
+    std::vector<JitKernel> ks;
+    for (const OshmProgram* pr : progs) {
+        int t = 0;
+        size_t sm = 0;
+        const std::string src = generate(*pr, t, sm, shape0);
+        std::shared_ptr<CacheEntry> e;
+        {
+            std::lock_guard<std::mutex> lk(g_cache_mu);
+            auto it = g_cache.find(src);
+            if (it == g_cache.end()) return false;
+            e = it->second;
+        }
+        std::lock_guard<std::mutex> lk(e->m);
+        if (e->pending || !e->ok) return false;
+        ks.push_back(e->k);
+    }
+    out.swap(ks);
+    return true;
 }
 
 void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, int* err, cudaStream_t st) {

@@ -23,6 +23,9 @@ struct JitKernel {
 bool jit_available();
 // Compile (or fetch from the process-wide cache) one kernel per program.
 std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>& progs);
+// The kernels of every program when all are compiled already; false otherwise
+// (nothing is compiled).
+bool jit_lookup_cached(const std::vector<const OshmProgram*>& progs, std::vector<JitKernel>& out);
 // `err`: the device error word (a RING kernel records a timed-out wait there)
 void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, int* err, cudaStream_t st);
 std::string jit_source(const OshmProgram& prog);

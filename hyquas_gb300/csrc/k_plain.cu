@@ -1,8 +1,8 @@
 // Plain-path kernels: one launch per gate (the reference's BACKEND=serial,
 // src/kernelSimple.cu:335-446), |0..0> initialisation (src/kernelSimple.cu:9-37),
 // FP64 probability reductions (src/kernelSimple.cu:467-516), amplitude gather
-// (src/kernelSimple.cu:518-522) and the in-HBM qubit remaps (one bit exchange
-// in place, or a whole permutation in one out-of-place pass).
+// (src/kernelSimple.cu:518-522) and the in-HBM qubit remaps (one bit exchange,
+// or a permutation of up to 13 tile bits per pass, in place).
 //
 // All indices are 64-bit (the reference's `int nVec` overflows at n >= 32,
 // src/kernelSimple.cu:338).  Every kernel is HBM-bound.
@@ -309,6 +309,7 @@ struct PermuteParams {
     uint64_t ntiles;
 };
 
+// Any tile size (used below 2^10 amplitudes): one amplitude per access.
 __global__ void __launch_bounds__(256) k_permute_bits(float2* __restrict__ a,
                                                       const __grid_constant__ PermuteParams p) {
     extern __shared__ float2 tile[];
@@ -325,6 +326,46 @@ __global__ void __launch_bounds__(256) k_permute_bits(float2* __restrict__ a,
             const int j = p.wr_lo[w & 31] | p.wr_mid[(w >> 5) & 31] | p.wr_hi[w >> 10];
             a[base + p.dst_lo[j & 31] + p.dst_mid[(j >> 5) & 31] + p.dst_hi[j >> 10]] =
                 tile[j ^ p.swz_mid[(j >> 5) & 31] ^ p.swz_hi[j >> 10]];
+        }
+        __syncthreads();
+    }
+}
+
+// Tiles of 2^K amplitudes, K = 10..13: 16-byte accesses (local index bit 0 is
+// source bit 0 and write-order bit 0 lands on destination bit 0, so index
+// pairs 2i, 2i+1 are neighbours on both sides), and every load of a tile is
+// issued before the first shared-memory store so that 2^K / 512 loads per
+// thread can be in flight at once.
+template <int K>
+__global__ void __launch_bounds__(256) k_permute_tile(float2* __restrict__ a,
+                                                      const __grid_constant__ PermuteParams p) {
+    constexpr int PP = (1 << K) / 512;  // index pairs per thread
+    extern __shared__ float2 tile[];
+    const int t = threadIdx.x;
+    auto src = [&](int e) { return p.src_lo[e & 31] + p.src_mid[(e >> 5) & 31] + p.src_hi[e >> 10]; };
+    auto dst = [&](int j) { return p.dst_lo[j & 31] + p.dst_mid[(j >> 5) & 31] + p.dst_hi[j >> 10]; };
+    auto slot = [&](int j) { return j ^ p.swz_mid[(j >> 5) & 31] ^ p.swz_hi[j >> 10]; };
+    for (uint64_t u = blockIdx.x; u < p.ntiles; u += gridDim.x) {
+        uint64_t base = 0;
+        for (int r = 0; r < p.nrest; r++) base |= ((u >> r) & 1) << p.rest[r];
+        float4 v[PP];
+#pragma unroll
+        for (int m = 0; m < PP; m++)
+            v[m] = __ldcs(reinterpret_cast<const float4*>(a + base + src(2 * (t + 256 * m))));
+#pragma unroll
+        for (int m = 0; m < PP; m++) {
+            const int e = 2 * (t + 256 * m);
+            tile[slot(e)] = make_float2(v[m].x, v[m].y);
+            tile[slot(e + 1)] = make_float2(v[m].z, v[m].w);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < PP; m++) {
+            const int w = 2 * (t + 256 * m);
+            const int j0 = p.wr_lo[w & 31] | p.wr_mid[(w >> 5) & 31] | p.wr_hi[w >> 10];
+            const int j1 = p.wr_lo[(w + 1) & 31] | p.wr_mid[(w >> 5) & 31] | p.wr_hi[w >> 10];
+            const float2 x0 = tile[slot(j0)], x1 = tile[slot(j1)];
+            __stcs(reinterpret_cast<float4*>(a + base + dst(j0)), make_float4(x0.x, x0.y, x1.x, x1.y));
         }
         __syncthreads();
     }
@@ -425,17 +466,36 @@ PermuteParams make_permute_params(int n, const int* dest_of) {
     return p;
 }
 
+template <int K>
+void launch_permute_tile(void* state, const PermuteParams& p, cudaStream_t st) {
+    const int smem = int(sizeof(float2) << K);
+    static std::once_flag once;
+    static int per_sm = 1;
+    std::call_once(once, [&] {
+        HQ_CHECK_CUDA(cudaFuncSetAttribute(k_permute_tile<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        HQ_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_permute_tile<K>, 256, smem));
+        if (per_sm < 1) per_sm = 1;
+    });
+    const uint64_t cap = uint64_t(ctx().sm_count) * per_sm;
+    const unsigned grid = (unsigned)(p.ntiles < cap ? p.ntiles : cap);
+    k_permute_tile<K><<<grid, 256, smem, st>>>((float2*)state, p);
+}
+
 void launch_permute_bits(void* state, int n, const int* dest_of, void* stream) {
     const PermuteParams p = make_permute_params(n, dest_of);
-    const size_t smem = sizeof(float2) << p.tile_bits;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        HQ_CHECK_CUDA(cudaFuncSetAttribute(k_permute_bits, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           int(sizeof(float2) << kPermuteMaxTileBits)));
-    });
-    const uint64_t cap = uint64_t(ctx().sm_count) * 3;
-    const unsigned grid = (unsigned)(p.ntiles < cap ? p.ntiles : cap);
-    k_permute_bits<<<grid, 256, smem, (cudaStream_t)stream>>>((float2*)state, p);
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (p.tile_bits) {
+        case 10: launch_permute_tile<10>(state, p, st); break;
+        case 11: launch_permute_tile<11>(state, p, st); break;
+        case 12: launch_permute_tile<12>(state, p, st); break;
+        case 13: launch_permute_tile<13>(state, p, st); break;
+        default: {
+            const size_t smem = sizeof(float2) << p.tile_bits;  // at most 8 KiB here
+            const uint64_t cap = uint64_t(ctx().sm_count) * 4;
+            const unsigned grid = (unsigned)(p.ntiles < cap ? p.ntiles : cap);
+            k_permute_bits<<<grid, 256, smem, st>>>((float2*)state, p);
+        }
+    }
     HQ_CHECK_CUDA(cudaGetLastError());
 }
 

@@ -163,7 +163,7 @@ void schedule_deserialize(const uint8_t* buf, size_t len, hq_circuit_s* c) {
     o.mm_precision = r.get<int32_t>();
     o.reference_grouping = r.get<int32_t>();
     o.specialize = r.get<int32_t>();
-    HQ_REQUIRE(o.specialize >= 0 && o.specialize <= 2, HQ_ERR_INVALID, "schedule bytes: specialize %d",
+    HQ_REQUIRE(o.specialize >= 0 && o.specialize <= 3, HQ_ERR_INVALID, "schedule bytes: specialize %d",
                o.specialize);
     config_from_options(o, n);  // checks the options
     const size_t max_gates = (len - r.at) / (16 + 64);

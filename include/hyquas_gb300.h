@@ -206,7 +206,11 @@ typedef struct hq_compile_options {
     int32_t specialize;    /* OShareMem kernels: 0 = interpreter (runs of single-qubit gates
                               on a qubit are fused into one gate first), 1 = one generated
                               kernel per group (NVRTC, error if unavailable), 2 = generated
-                              when NVRTC is present, else interpreter (default) */
+                              when NVRTC is present, else interpreter (default), 3 = as 2
+                              but kernels not compiled before are compiled on a host thread
+                              after compile returns; runs use the interpreter for the
+                              groups until their kernels are in (a new circuit's first run
+                              does not wait for NVRTC) */
 } hq_compile_options;
 
 /* OShareMem backend, autotuned widths, split BF16, generated kernels when
