@@ -702,6 +702,61 @@ def run_batch(args, dist: Dist):
         print(json.dumps(line), flush=True)
 
 
+def run_dense28(args, dist: Dist):
+    """The 20-qubit plain-path circuit family (U3 on every qubit, then CNOT on
+    a random matching, per layer) at 28 qubits: every single-qubit gate is a
+    general complex 2x2, the case where fused TransMM groups can beat
+    OShareMem.  OShareMem-only, TransMM-only and the hybrid choice, each
+    against the FP64 oracle."""
+    import hyquas_gb300 as hq
+    from hyquas_gb300 import workloads as W
+    import oracle as O
+    hq.init(dist.local)
+    n = args.dense_qubits
+    desc = W.plain_u3_cnot(1, n, args.dense_layers)
+    gates = W.to_gates(desc)
+    ref = O.run_f64(n, desc)
+    state = hq.State(n)
+    got = np.empty(1 << n, dtype=np.complex64)
+    rows = []
+    for backend in ("oshm", "hybrid", "transmm"):
+        c = hq.Circuit(n)
+        c.addGates(gates)
+        c.compile(backend)
+        kinds = [b for (b, _, _, _) in c.schedule()]
+        for _ in range(max(args.warmup, 1)):
+            state.init_zero()
+            c.run_on(state)
+        ts = []
+        for _ in range(args.steps):
+            state.init_zero()
+            ts.append(c.run_on(state))
+        state.init_zero()
+        c.run_on(state)
+        state.store(got)
+        acc = O.compare(ref, got)
+        rows.append({"backend": backend, "ms": float(np.median(ts)) / 1000.0,
+                     "passes": len(kinds), "transmm_groups": sum(1 for b in kinds if b == hq.BACKEND_TRANSMM),
+                     "predicted_ms": float(np.sum(c.predict())) / 1000.0, **acc})
+        if dist.rank == 0:
+            print(json.dumps({"dense_case": rows[-1]}), file=sys.stderr, flush=True)
+    best = min(rows, key=lambda r: r["ms"])
+    peak, peak_kind = measured_peaks()
+    achieved = best["passes"] * 16.0 * (1 << n) / (best["ms"] * 1e-3) / 1e9
+    line = base_line(args, dist, f"{n}q U3+CNOT circuit time (ms), best backend", best["ms"], "ms",
+                     best["ms"], False,
+                     f"{n} qubits, {args.dense_layers} layers of U3 on every qubit + CNOT on a random "
+                     "matching, |0..0>; OShareMem-only, hybrid and TransMM-only (split BF16, 7-qubit "
+                     "groups), each checked against the FP64 oracle",
+                     {"cases": rows, "best_backend": best["backend"]})
+    line.update({"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                              "frac": achieved / peak, "traffic": None,
+                              "kernel": "circuit average over its passes", "peak_source": peak_kind},
+                 "cpu_baseline": None, "e2e": None, "gpu_launches": best["passes"] * args.steps})
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_remap(args, dist: Dist):
     """In-HBM qubit remap (the single-GPU form of the reference's global-qubit
     exchange, src/executor.cpp:59-179): a step moves 8 physical bits of a
@@ -912,7 +967,9 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP64 oracle comparison (grid30: about a minute of CPU)")
     ap.add_argument("--workload", default="grid30",
-                    choices=["grid30", "plain20", "qft28", "batch", "serve", "remap"])
+                    choices=["grid30", "plain20", "qft28", "batch", "serve", "remap", "dense28"])
+    ap.add_argument("--dense-qubits", type=int, default=28)
+    ap.add_argument("--dense-layers", type=int, default=10)
     ap.add_argument("--remap-qubits", type=int, default=30)
     ap.add_argument("--qft-qubits", type=int, default=28)
     ap.add_argument("--qft-cases", default="",
@@ -933,7 +990,7 @@ def main():
             run_ours(args, dist)
         else:
             {"plain20": run_plain20, "qft28": run_qft28, "batch": run_batch,
-             "serve": run_serve, "remap": run_remap}[args.workload](args, dist)
+             "serve": run_serve, "remap": run_remap, "dense28": run_dense28}[args.workload](args, dist)
     finally:
         dist.close()
 

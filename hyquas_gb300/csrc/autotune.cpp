@@ -6,9 +6,10 @@
 // Here one call times single-group circuits on a scratch state with CUDA
 // events, through the same compiled path a user's circuit takes, and fits:
 //   pass_floor      one OShareMem group with a single Z gate
-//   oshm_gate       slope of a group of RX gates on its tile qubits
-//   oshm_diag       added slope of T gates interleaved with those RX gates
-//   oshm_ctrl_diag  added slope of CU1 gates interleaved with them
+//   oshm_gate       arithmetic of a group of RX gates on its tile qubits
+//   oshm_diag       added arithmetic of T gates interleaved with those RX gates
+//   oshm_ctrl_diag  added arithmetic of CU1 gates interleaved with them
+// (group time = amps * sqrt(pass_floor^2 + arithmetic^2), compiler.cpp)
 //   mm_*            one 6-qubit TransMM group per precision
 //   launch          a one-tile group (13 qubits)
 #include <algorithm>
@@ -79,10 +80,12 @@ hq_cost_params autotune(int n) {
         const double t_nd = time_circuit(s, nd, o);
         const double t_dg = time_circuit(s, dg, o);
         const double t_cd = time_circuit(s, cd, o);
+        // cost_oshm: t = amps * sqrt(floor^2 + work^2) per group
+        auto work = [&](double t) { return std::sqrt(std::max(0.0, t * t - floor * floor)) / amps; };
         p.pass_floor = floor / amps;
-        p.oshm_gate = std::max(0.0, t_nd - floor) / (G * amps);
-        p.oshm_diag = std::max(0.0, t_dg - t_nd) / (G * amps);
-        p.oshm_ctrl_diag = std::max(0.0, t_cd - t_nd) / (G * amps);
+        p.oshm_gate = work(t_nd) / (G * oshm_gate_units(nd[0]));  // per unit (RX: 2)
+        p.oshm_diag = std::max(0.0, work(t_dg) - work(t_nd)) / G;
+        p.oshm_ctrl_diag = std::max(0.0, work(t_cd) - work(t_nd)) / G;
         // TransMM: 6-qubit groups on qubits 0..5
         std::vector<hq_gate> mm;
         for (int i = 0; i < 24; i++) mm.push_back(gate(G_RY, i % 6, -1, 0.3 + 0.05 * i));

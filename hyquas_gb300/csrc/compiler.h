@@ -50,6 +50,7 @@ hq_cost_params cost_params();
 void set_cost_params(const hq_cost_params& p);
 hq_cost_params autotune(int n);  // autotune.cpp: measure and install the parameters
 double cost_oshm(int n, int nphases, const std::vector<hq_gate>& gates, int k);
+double oshm_gate_units(const hq_gate& g);  // arithmetic weight of a non-diagonal gate
 double cost_transmm(int n, int m, int precision);
 
 // ---- OShareMem lowering ------------------------------------------------------

@@ -83,7 +83,9 @@ hq_status hq_set_hbm_budget(uint64_t bytes);
 /* Device bytes the library holds (states, programs, scratch). */
 hq_status hq_hbm_in_use(uint64_t* bytes);
 
-/* Page-locked host buffers for fast state transfers (cudaHostAlloc). */
+/* Page-locked host buffers for fast state transfers: from 64 MiB up an
+ * anonymous mapping with transparent huge pages requested, page-locked with
+ * cudaHostRegister; smaller ones (or where that fails) from cudaHostAlloc. */
 hq_status hq_host_alloc(uint64_t bytes, void** out);
 /* Frees a buffer from hq_host_alloc. */
 hq_status hq_host_free(void* p);

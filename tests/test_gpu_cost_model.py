@@ -42,7 +42,8 @@ def test_predicted_group_times_track_measured(hq, name):
     ratio = pred / meas
     # every group within a factor 1.6 of its measured time, the circuit's total
     # within 25 %, and (with enough groups to rank) the same order of cost
-    assert np.all((ratio > 1 / 1.6) & (ratio < 1.6)), (name, pred.tolist(), meas.tolist())
-    assert abs(pred.sum() / meas.sum() - 1) < 0.25, (name, pred.sum(), meas.sum())
+    msg = f"{name}: predicted {np.round(pred).tolist()} measured {np.round(meas).tolist()} us"
+    assert np.all((ratio > 1 / 1.6) & (ratio < 1.6)), msg
+    assert abs(pred.sum() / meas.sum() - 1) < 0.25, msg
     if len(meas) >= 5 and np.ptp(meas) > 0.2 * np.mean(meas):
-        assert spearman(pred, meas) >= 0.6, (name, pred.tolist(), meas.tolist())
+        assert spearman(pred, meas) >= 0.6, msg
