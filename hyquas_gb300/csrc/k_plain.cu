@@ -305,6 +305,7 @@ struct PermuteParams {
     uint16_t swz_mid[32], swz_hi[8];
     uint8_t rest[64];   // tile-index bit r -> its (unmoved) physical bit
     int nrest;
+    int pair_read;      // write-order bit 0 is local bit 0: index pairs are slot pairs
     int tile_bits;
     uint64_t ntiles;
 };
@@ -352,20 +353,25 @@ __global__ void __launch_bounds__(256) k_permute_tile(float2* __restrict__ a,
 #pragma unroll
         for (int m = 0; m < PP; m++)
             v[m] = __ldcs(reinterpret_cast<const float4*>(a + base + src(2 * (t + 256 * m))));
+        // the swizzle leaves slot bit 0 alone: index pair (e, e + 1) is slot pair
+        // (slot(e), slot(e) + 1), one 16-byte store
 #pragma unroll
-        for (int m = 0; m < PP; m++) {
-            const int e = 2 * (t + 256 * m);
-            tile[slot(e)] = make_float2(v[m].x, v[m].y);
-            tile[slot(e + 1)] = make_float2(v[m].z, v[m].w);
-        }
+        for (int m = 0; m < PP; m++)
+            *reinterpret_cast<float4*>(tile + slot(2 * (t + 256 * m))) = v[m];
         __syncthreads();
 #pragma unroll
         for (int m = 0; m < PP; m++) {
             const int w = 2 * (t + 256 * m);
             const int j0 = p.wr_lo[w & 31] | p.wr_mid[(w >> 5) & 31] | p.wr_hi[w >> 10];
-            const int j1 = p.wr_lo[(w + 1) & 31] | p.wr_mid[(w >> 5) & 31] | p.wr_hi[w >> 10];
-            const float2 x0 = tile[slot(j0)], x1 = tile[slot(j1)];
-            __stcs(reinterpret_cast<float4*>(a + base + dst(j0)), make_float4(x0.x, x0.y, x1.x, x1.y));
+            float4 x;
+            if (p.pair_read) {
+                x = *reinterpret_cast<const float4*>(tile + slot(j0));
+            } else {
+                const int j1 = p.wr_lo[(w + 1) & 31] | p.wr_mid[(w >> 5) & 31] | p.wr_hi[w >> 10];
+                const float2 x0 = tile[slot(j0)], x1 = tile[slot(j1)];
+                x = make_float4(x0.x, x0.y, x1.x, x1.y);
+            }
+            __stcs(reinterpret_cast<float4*>(a + base + dst(j0)), x);
         }
         __syncthreads();
     }
@@ -435,23 +441,25 @@ PermuteParams make_permute_params(int n, const int* dest_of) {
     fillw(p.wr_mid, 32, 5);
     fillw(p.wr_hi, 8, 10);
     // swizzle: local bits >= 5 that vary across a destination-order warp fold
-    // onto slot bits 0-4 that do not vary there; the other high bits fold onto
-    // slot bits 0-4 in turn
+    // onto slot bits 1-4 that do not vary there; the other high bits fold onto
+    // slot bits 1-4 in turn.  Slot bit 0 is never folded, so index pairs
+    // (2i, 2i + 1) stay slot pairs.
     int target[kPermuteMaxTileBits];
     for (int j = 0; j < K; j++) target[j] = -1;
-    uint32_t taken = 0;
+    uint32_t taken = 1u;
     for (int b = 0; b < c && b < nw; b++)
         if (wbit[b] < 5) taken |= 1u << wbit[b];
     for (int b = 0; b < c && b < nw; b++)
         if (wbit[b] >= 5)
-            for (int f = 0; f < 5; f++)
+            for (int f = 1; f < 5; f++)
                 if (!((taken >> f) & 1)) {
                     target[wbit[b]] = f;
                     taken |= 1u << f;
                     break;
                 }
     for (int j = 5; j < K; j++)
-        if (target[j] < 0) target[j] = (j - 5) % 5;
+        if (target[j] < 0) target[j] = 1 + (j - 5) % 4;
+    p.pair_read = (nw > 0 && wbit[0] == 0) ? 1 : 0;
     for (int m = 0; m < 32; m++)
         for (int b = 0; b < 5; b++)
             if (((m >> b) & 1) && 5 + b < K) p.swz_mid[m] ^= uint16_t(1) << target[5 + b];
