@@ -280,8 +280,58 @@ Partition partition_greedy(int n, const std::vector<hq_gate>& gates, const std::
 // dependencies of a reversed circuit are the reversed ones, so the played-back
 // groups are a valid schedule); the one with fewer passes is kept, the
 // forward one on a tie.  The reference's grouping is only the forward greedy.
+namespace {
+Partition partition_width(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
+                          const CompileConfig& cfg);
+}  // namespace
+
+// The cost model's device time of a partition (seconds).
+double predicted_time(int n, const std::vector<hq_gate>& gates, const Partition& part,
+                      const CompileConfig& cfg) {
+    double t = 0;
+    for (const GroupPlan& gp : part.groups) {
+        if (gp.backend == HQ_BACKEND_OSHM) {
+            std::vector<hq_gate> gs;
+            for (int x : gp.gates) gs.push_back(gates[x]);
+            t += cost_oshm(n, 0, gs, gp.width);
+        } else {
+            t += cost_transmm(n, gp.width, cfg.mm_precision);
+        }
+    }
+    return t;
+}
+
+// With tile_auto the OShareMem tile width is chosen per circuit: the circuit
+// is partitioned at 11, 12 and 13 tile qubits and the partition the cost
+// model predicts fastest is kept (narrower tiles mean more passes but can
+// group the same gates differently).  The reference reads per-qubit-count
+// parameter files for this instead (src/evaluator.cpp:60-109).
 Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
                     const CompileConfig& cfg) {
+    if (!cfg.tile_auto || cfg.reference || cfg.backend == HQ_BACKEND_TRANSMM)
+        return partition_width(n, gates, pos0, cfg);
+    Partition best;
+    double best_t = 0;
+    bool have = false;
+    for (int t = 13; t >= 11; t--) {
+        if (t > n && have) continue;
+        CompileConfig c = cfg;
+        c.tile = std::min(t, n);
+        Partition p = partition_width(n, gates, pos0, c);
+        const double pt = predicted_time(n, gates, p, c);
+        if (!have || pt < best_t * (1 - 1e-9)) {
+            best = std::move(p);
+            best_t = pt;
+            have = true;
+        }
+        if (t > n) break;
+    }
+    return best;
+}
+
+namespace {
+Partition partition_width(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
+                          const CompileConfig& cfg) {
     Partition fwd = partition_greedy(n, gates, pos0, cfg);
     if (cfg.reference || gates.size() < 2) return fwd;
     const int N = (int)gates.size();
@@ -298,6 +348,7 @@ Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<
     out.final_pos = fwd.final_pos;  // layouts stay the identity outside reference grouping
     return out;
 }
+}  // namespace
 
 namespace {
 Partition partition_greedy(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,

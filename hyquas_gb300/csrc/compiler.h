@@ -23,6 +23,7 @@ struct CompileConfig {
     int mm_qubits = 6;   // TransMM width
     int mm_precision = HQ_MM_BF16X3;
     bool reference = false;
+    bool tile_auto = false;  // choose the tile width (11..13) by predicted time
 };
 
 struct GroupPlan {
@@ -43,6 +44,10 @@ struct Partition {
 // initial layout is `pos0` (logical -> physical).
 Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
                     const CompileConfig& cfg);
+
+// The cost model's device time (seconds) of a partition of `gates`.
+double predicted_time(int n, const std::vector<hq_gate>& gates, const Partition& part,
+                      const CompileConfig& cfg);
 
 // GB300 cost model (seconds) used by the hybrid backend; the constants are
 // fitted to kernel timings on GB300 (compiler.cpp).

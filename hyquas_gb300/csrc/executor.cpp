@@ -342,6 +342,7 @@ CompileConfig config_from_options(const hq_compile_options& o, int n) {
     cfg.backend = o.backend;
     cfg.reference = o.reference_grouping != 0;
     cfg.tile = o.tile_qubits > 0 ? o.tile_qubits : 13;
+    cfg.tile_auto = o.tile_qubits == 0;
     cfg.coalesce = o.coalesce > 0 ? o.coalesce : 3;
     // tensor-core passes cost the same at 6 and 7 qubits (measured), so the
     // wider group is the default there; FP32 SIMT doubles its cost per qubit

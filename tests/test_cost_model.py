@@ -51,3 +51,18 @@ def test_autotune_measures_plausible_constants(hq):
         assert 0 < p["launch"] < 1e-3, p
     finally:
         hq.set_cost_params(p0)
+
+
+def test_tile_width_is_chosen_per_circuit():
+    """tile_qubits = 0 partitions at 11, 12 and 13 tile qubits and keeps the
+    partition the cost model predicts fastest; an explicit width is kept."""
+    import hyquas_gb300 as hq
+    from hyquas_gb300 import workloads as W
+    g = W.to_gates(W.grid_random(2, 5, 6, 20))
+    auto = hq.plan_groups(30, g)
+    assert {x["width"] for x in auto} == {13} and len(auto) == 11
+    for t in (11, 12):
+        fixed = hq.plan_groups(30, g, tile_qubits=t)
+        assert {x["width"] for x in fixed} == {t} and len(fixed) > len(auto)
+    small = hq.plan_groups(9, W.to_gates(W.grid_random(3, 3, 3, 6)))
+    assert {x["width"] for x in small} == {9}
