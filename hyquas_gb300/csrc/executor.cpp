@@ -1,6 +1,7 @@
 #include "executor.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "common.h"
@@ -282,10 +283,13 @@ void apply_oshm_group(hq_state_s* s, const std::vector<hq_gate>& gates, uint64_t
 
 // ---- circuits ---------------------------------------------------------------------
 
-// Background compiles of released circuits run on (their kernels still land in
-// the process-wide cache for later circuits); finished ones are joined at the
-// next release and the rest when the library unloads.
-struct OrphanJobs {
+// Every background compile is registered here.  A released circuit does not
+// wait for its kernels (they still land in the process-wide cache); finished
+// jobs are dropped at the next registration or release, and the ones still
+// running are joined by an exit hook registered with atexit when the first
+// job starts -- after the CUDA runtime's own registration, so it runs before
+// the runtime tears down.
+struct JobRegistry {
     std::mutex mu;
     std::vector<std::shared_ptr<JitJob>> jobs;
     void prune() {
@@ -297,27 +301,28 @@ struct OrphanJobs {
                 done = jobs[i]->done;
             }
             if (done) {
-                if (jobs[i]->th.joinable()) jobs[i]->th.join();
+                jobs[i]->join();
                 jobs.erase(jobs.begin() + i);
             } else {
                 i++;
             }
         }
     }
-    ~OrphanJobs() {
-        for (auto& j : jobs)
-            if (j->th.joinable()) j->th.join();
-    }
 };
-OrphanJobs g_orphans;
+JobRegistry g_jobs;
+
+void join_background_compiles() {
+    std::vector<std::shared_ptr<JitJob>> jobs;
+    {
+        std::lock_guard<std::mutex> lk(g_jobs.mu);
+        jobs.swap(g_jobs.jobs);
+    }
+    for (auto& j : jobs) j->join();
+}
 
 void circuit_release(hq_circuit_s* c) {
-    if (c->jit_job) {
-        std::lock_guard<std::mutex> lk(g_orphans.mu);
-        g_orphans.jobs.push_back(c->jit_job);
-        c->jit_job.reset();
-    }
-    g_orphans.prune();
+    c->jit_job.reset();  // the registry keeps it until it is done
+    g_jobs.prune();
     if (c->graph) cudaGraphExecDestroy(c->graph);
     c->graph = nullptr;
     c->graph_state = nullptr;
@@ -483,6 +488,8 @@ void circuit_lower(hq_circuit_s* c) {
                 } else {
                     // background mode, kernels not compiled yet: compile them on a
                     // host thread; until they are in, the interpreter runs the groups
+                    static std::once_flag exit_hook;
+                    std::call_once(exit_hook, [] { std::atexit(join_background_compiles); });
                     auto job = std::make_shared<JitJob>();
                     for (const OshmProgram* pr : progs) job->progs.push_back(*pr);
                     job->groups = idx;
@@ -503,6 +510,11 @@ void circuit_lower(hq_circuit_s* c) {
                         jp->err = err;
                         jp->done = true;
                     });
+                    g_jobs.prune();
+                    {
+                        std::lock_guard<std::mutex> lk(g_jobs.mu);
+                        g_jobs.jobs.push_back(job);
+                    }
                     c->jit_job = job;
                 }
             } catch (const Failure& f) {
@@ -521,7 +533,7 @@ void circuit_jit_install(hq_circuit_s* c, bool wait) {
         std::lock_guard<std::mutex> lk(job->mu);
         if (!job->done && !wait) return;
     }
-    if (job->th.joinable()) job->th.join();
+    job->join();
     c->jit_job.reset();
     if (!job->err.empty() || job->kernels.size() != job->groups.size()) {
         c->specialize_note = job->err.empty() ? "specialisation failed" : job->err;

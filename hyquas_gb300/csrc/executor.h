@@ -34,11 +34,16 @@ namespace hq {
 struct JitJob {
     std::thread th;
     std::mutex mu;
+    std::mutex join_mu;             // joins from the installing run and the exit hook
     bool done = false;
     std::vector<OshmProgram> progs;
     std::vector<size_t> groups;     // dgroups index of each program
     std::vector<JitKernel> kernels;
     std::string err;
+    void join() {
+        std::lock_guard<std::mutex> lk(join_mu);
+        if (th.joinable()) th.join();
+    }
 };
 
 struct DeviceGroup {

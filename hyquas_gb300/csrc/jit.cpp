@@ -558,8 +558,11 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
     g.nv = NV;
     std::ostringstream& o = g.o;
     o << kPrelude;
+    // PAIRED and RING keep 128 registers per thread: RING with narrower tiles
+    // (fewer threads per CTA) asks for as many CTAs per SM as fill 64K registers
+    const int ring_min_blocks = std::max(1, 65536 / (threads * 128));
     o << "extern \"C\" __global__ void __launch_bounds__(" << threads
-      << (paired ? ", 2" : ring ? ", 1" : "")
+      << (paired ? ", 2" : ring ? ", " + std::to_string(ring_min_blocks) : std::string(""))
       << ") hq_oshm_group(float2* __restrict__ state, u64 ntiles, int* __restrict__ err) {\n";
     if (ring)
         o << "extern __shared__ float4 smem4[];\nconst unsigned grp = threadIdx.x / " << T
@@ -904,7 +907,7 @@ std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>&
                     // a spill of up to 128 bytes per thread costs less than the 16
                     // warps per SM gain (measured on the 30-qubit grid); beyond that,
                     // one double-buffered CTA of 8 warps per SM
-                    const int need = shape0 == Shape::PAIRED ? 2 : 1;
+                    const int need = shape0 == Shape::PAIRED ? 2 : 1;  // RING: bounds ask for more
                     if (shape0 != Shape::SINGLE && (jk.local_bytes > 128 || jk.blocks_per_sm < need)) {
                         cudaLibraryUnload(jk.lib);
                         int t2 = 0;
