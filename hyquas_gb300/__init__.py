@@ -105,6 +105,7 @@ def _load():
         "hq_circuit_schedule": [P, C.POINTER(I32), P, P, P, P],
         "hq_circuit_group_gates": [P, I32, P, I32, C.POINTER(I32)],
         "hq_circuit_run": [P, P, C.POINTER(D)],
+        "hq_circuit_run_to_host": [P, P, P, C.POINTER(D)],
         "hq_circuit_enqueue": [P, P],
         "hq_circuit_profile": [P, P, P],
         "hq_circuit_predict": [P, P],
@@ -654,6 +655,16 @@ class Circuit:
     def run_on(self, state: State) -> float:
         us = C.c_double()
         check(lib.hq_circuit_run(self._h, state.handle, C.byref(us)))
+        return us.value
+
+    def run_to_host(self, state: State, out: np.ndarray) -> float:
+        """Run on `state` and leave the final state (logical order) in `out`, a
+        complex64 array of 2^n entries; device time in us.  With a pinned
+        `out` (PinnedBuffer.array) the last group writes it in the same pass."""
+        if out.dtype != np.complex64 or out.size != (1 << self.numQubits) or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous complex64 array of 2^n amplitudes")
+        us = C.c_double()
+        check(lib.hq_circuit_run_to_host(self._h, state.handle, C.c_void_p(out.ctypes.data), C.byref(us)))
         return us.value
 
     def profile(self, state: State) -> np.ndarray:

@@ -545,6 +545,16 @@ hq_status hq_circuit_run(hq_circuit c, hq_state s, double* elapsed_us) {
     HQ_API_END
 }
 
+hq_status hq_circuit_run_to_host(hq_circuit c, hq_state s, float* host_amps, double* elapsed_us) {
+    HQ_API_BEGIN
+    HQ_NONNULL(c);
+    HQ_NONNULL(s);
+    HQ_NONNULL(host_amps);
+    const double us = circuit_run_to_host(c, s, host_amps);
+    if (elapsed_us) *elapsed_us = us;
+    HQ_API_END
+}
+
 hq_status hq_circuit_profile(hq_circuit c, hq_state s, double* group_us) {
     HQ_API_BEGIN
     HQ_NONNULL(c);

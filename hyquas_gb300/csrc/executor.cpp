@@ -601,6 +601,72 @@ double circuit_run(hq_circuit_s* c, hq_state_s* s, bool sync) {
     return double(ms) * 1000.0;
 }
 
+// A run that also leaves the final state, in logical order, at `host` (the
+// reference's run followed by its full-state readback, src/circuit.cpp:46-62).
+// When the last group is a generated kernel, the run ends in the canonical
+// layout and `host` is pinned, that group writes every finished amplitude to
+// HBM and to `host` (one pass, no separate copy); otherwise the run is
+// followed by a copy.  Returns the device time of the run including the
+// readback, in microseconds.
+double circuit_run_to_host(hq_circuit_s* c, hq_state_s* s, void* host) {
+    HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
+    HQ_REQUIRE(s->n == c->n, HQ_ERR_INVALID, "state has %d qubits, circuit %d", s->n, c->n);
+    circuit_jit_install(c, false);
+    bool fused = c->opt.backend != HQ_BACKEND_PLAIN && c->n >= 6 && !c->dgroups.empty() &&
+                 c->dgroups.back().backend == HQ_BACKEND_OSHM && c->dgroups.back().has_jit;
+    for (int q = 0; fused && q < c->n; q++) fused = c->swap_perm[q] == q;
+    void* dhost = nullptr;
+    if (fused) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, host) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+            a.devicePointer != nullptr)
+            dhost = a.devicePointer;
+        else
+            cudaGetLastError();  // not pinned: the copy path below
+        fused = dhost != nullptr;
+    }
+    cudaStream_t st = ctx().stream;
+    if (!fused) {
+        circuit_run(c, s, false);
+        state_canonicalize(s);
+        HQ_CHECK_CUDA(cudaMemcpyAsync(host, s->d, s->bytes, cudaMemcpyDeviceToHost, st));
+        HQ_CHECK_CUDA(cudaEventRecord(c->ev1, st));
+        HQ_CHECK_CUDA(cudaEventSynchronize(c->ev1));
+        check_device_error();
+        float ms = 0.f;
+        HQ_CHECK_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+        return double(ms) * 1000.0;
+    }
+    state_canonicalize(s);
+    if (!c->ev0) {
+        HQ_CHECK_CUDA(cudaEventCreate(&c->ev0));
+        HQ_CHECK_CUDA(cudaEventCreate(&c->ev1));
+    }
+    HQ_CHECK_CUDA(cudaEventRecord(c->ev0, st));
+    const size_t ng = c->dgroups.size();
+    for (size_t g = 0; g < ng; g++) {
+        const DeviceGroup& dg = c->dgroups[g];
+        if (g + 1 == ng) {
+            jit_launch(dg.jit, s->d, uint64_t(1) << (c->n - dg.prog.k), ctx().d_error, st, dhost);
+        } else if (dg.backend == HQ_BACKEND_OSHM && dg.has_jit) {
+            jit_launch(dg.jit, s->d, uint64_t(1) << (c->n - dg.prog.k), ctx().d_error, st);
+        } else if (dg.backend == HQ_BACKEND_OSHM) {
+            OshmLaunch p = make_oshm_launch(dg.prog, s->d, c->d_phases + dg.phase_off, c->d_ops,
+                                            ctx().d_error);
+            launch_oshm(p, st);
+        } else {
+            transmm_launch(c, dg, s->d, st);
+        }
+    }
+    HQ_CHECK_CUDA(cudaEventRecord(c->ev1, st));
+    for (int q = 0; q < c->n; q++) s->pos[q] = c->swap_perm[q];
+    HQ_CHECK_CUDA(cudaEventSynchronize(c->ev1));
+    check_device_error();
+    float ms = 0.f;
+    HQ_CHECK_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    return double(ms) * 1000.0;
+}
+
 void circuit_predict(const hq_circuit_s* c, double* group_us) {
     HQ_REQUIRE(c->compiled, HQ_ERR_STATE, "circuit not compiled");
     for (size_t g = 0; g < c->dgroups.size(); g++) {

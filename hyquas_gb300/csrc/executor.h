@@ -126,6 +126,7 @@ std::vector<uint8_t> schedule_serialize(const hq_circuit_s* c);
 // parse and check `len` bytes into c's plan (gates, options, partition); no device work
 void schedule_deserialize(const uint8_t* buf, size_t len, hq_circuit_s* c);
 double circuit_run(hq_circuit_s* c, hq_state_s* s, bool sync);
+double circuit_run_to_host(hq_circuit_s* c, hq_state_s* s, void* host);
 void circuit_capture(hq_circuit_s* c, hq_state_s* s);
 void circuit_profile(hq_circuit_s* c, hq_state_s* s, double* group_us);
 // the cost model's device time per group (us) of a compiled circuit

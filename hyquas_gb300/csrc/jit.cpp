@@ -103,6 +103,12 @@ DI float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a
 DI unsigned swz(unsigned x) { unsigned f = ((x >> 4) ^ (x >> 7) ^ (x >> 10) ^ (x >> 13)) & 7u; return x ^ (f << 1); }
 DI void cpa16(unsigned s, const void* g) { asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(g) : "memory"); }
 DI float F(unsigned b) { return __int_as_float((int)b); }
+// a finished amplitude pair to the state and, when the run also leaves a copy
+// of the final state in (device-mapped) host memory, to that copy
+DI void st_amps(float2* state, float2* copy, u64 idx, float4 w) {
+    *(float4*)(state + idx) = w;
+    if (copy) *(float4*)(copy + idx) = w;
+}
 // Bounded wait for phase `par` of the mbarrier at `addr`, decided by the whole
 // group (barrier `gbar`, `cnt` threads): either every thread of the group saw
 // the data land or none goes on.  After about two seconds the group records a
@@ -238,6 +244,43 @@ struct Gen {
                 bool k0, k1;
                 lanes(op.creg, j, k0, k1);
                 if ((k0 || k1) && pair_needs_align(kind, k0 && k1, has_cout)) align(j, j | (1 << (J - 1)));
+            }
+        }
+        // Sign flips under a run-time condition (CZ-like gates with a qubit
+        // outside the register set): a mask chosen by the condition and
+        // XORed in unconditionally, straight-line code that the compiler
+        // interleaves with the FMA-pipe arithmetic around it (a branch would
+        // keep the ALU work apart from it)
+        {
+            const bool dneg = kind == OP_DOUT && (op.flags & OPF_D0_ONE) && m[6] == -1.f && m[7] == 0.f &&
+                              op.creg != 0;
+            if ((kind == OP_NEGHI && has_cout) || dneg) {
+                std::string cond;
+                if (has_cout) cond = "(pidx & " + hex64(op.cout) + ") == " + hex64(op.cout);
+                if (dneg) cond += std::string(cond.empty() ? "" : " && ") + "(pidx & " + hex64(op.tout) + ") != 0ull";
+                o << "{ const u64 sg = (" << cond << ") ? 0x8000000080000000ull : 0ull;\n";
+                auto flip = [&](int j, bool k0, bool k1) {
+                    if (k0 && k1)
+                        o << R(j) << " ^= sg; " << I(j) << " ^= sg;\n";
+                    else if (k0 || k1) {
+                        const char* lm = k0 ? "0x80000000ull" : "0x8000000000000000ull";
+                        o << R(j) << " ^= sg & " << lm << "; " << I(j) << " ^= sg & " << lm << ";\n";
+                    }
+                };
+                for (int j = 0; j < nv; j++) {
+                    bool k0, k1;
+                    if (kind == OP_DOUT) {
+                        lanes(op.creg, j, k0, k1);
+                        flip(j, k0, k1);
+                    } else if (J == 0) {
+                        if ((uint32_t(2 * j) & op.creg) == op.creg) flip(j, false, true);
+                    } else if (!(j & (1 << (J - 1)))) {
+                        lanes(op.creg, j, k0, k1);
+                        flip(j | (1 << (J - 1)), k0, k1);
+                    }
+                }
+                o << "}\n";
+                return;
             }
         }
         if (has_cout) o << "if ((pidx & " << hex64(op.cout) << ") == " << hex64(op.cout) << ") {\n";
@@ -563,7 +606,8 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
     const int ring_min_blocks = std::max(1, 65536 / (threads * 128));
     o << "extern \"C\" __global__ void __launch_bounds__(" << threads
       << (paired ? ", 2" : ring ? ", " + std::to_string(ring_min_blocks) : std::string(""))
-      << ") hq_oshm_group(float2* __restrict__ state, u64 ntiles, int* __restrict__ err) {\n";
+      << ") hq_oshm_group(float2* __restrict__ state, u64 ntiles, int* __restrict__ err, "
+         "float2* __restrict__ copy) {\n";
     if (ring)
         o << "extern __shared__ float4 smem4[];\nconst unsigned grp = threadIdx.x / " << T
           << "u, t = threadIdx.x % " << T << "u, gbar = 1u + grp;\n";
@@ -758,7 +802,7 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
                 for (int b = 1; b < R; b++)
                     if ((j >> (b - 1)) & 1) off |= uint64_t(1) << tile_phys[P.r_local[b]];
                 o << "{ float4 w; vunpack(r" << j << ", w.x, w.z); vunpack(i" << j
-                  << ", w.y, w.w); *(float4*)(state + (pidx | " << hex64(off) << ")) = w; }\n";
+                  << ", w.y, w.w); st_amps(state, copy, pidx | " << hex64(off) << ", w); }\n";
             }
             o << "}\n";
             continue;
@@ -770,21 +814,26 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
             o << "((ulonglong2*)buf)[(sb" << p << " ^ " << c << "u) >> 1] = make_ulonglong2(r" << j
               << ", i" << j << ");\n";
         }
-        o << SYNC << "}\n";
+        // the next phase keeps the warp bits (thread bits 5..): each warp
+        // reads back only what it wrote, so a warp sync orders the exchange
+        bool warp_local = p + 1 < prog.phases.size() && K - R > 5;
+        for (int j = 5; warp_local && j < K - R; j++)
+            warp_local = P.g_local[j] == prog.phases[p + 1].g_local[j];
+        o << (warp_local ? std::string("__syncwarp();\n") : SYNC) << "}\n";
     }
     if (!direct) {
         // staged write-back; pieces are (re0, re1, im0, im1) after a phase and
         // as loaded when there is none
-        o << "float2* gdst = state + base + toff;\n";
+        o << "const u64 gdst = base + toff;\n";
         for (int m = 0; m < PPT; m++) {
             if (prog.phases.empty())
-                o << "*(float4*)(gdst + " << hex64(poff[m]) << ") = buf[(tslot ^ " << pslot[m]
-                  << "u) >> 1];\n";
+                o << "st_amps(state, copy, gdst + " << hex64(poff[m]) << ", buf[(tslot ^ " << pslot[m]
+                  << "u) >> 1]);\n";
             else
                 o << "{ const ulonglong2 q = ((const ulonglong2*)buf)[(tslot ^ " << pslot[m]
                   << "u) >> 1]; float4 w; vunpack(q.x, w.x, w.z); vunpack(q.y, w.y, w.w); "
-                     "*(float4*)(gdst + "
-                  << hex64(poff[m]) << ") = w; }\n";
+                     "st_amps(state, copy, gdst + "
+                  << hex64(poff[m]) << ", w); }\n";
         }
         o << SYNC;
         if (ring) o << "if (tile_of(i + 3) < ntiles) load_tile(tile_of(i + 3), bi, i + 3);\n";
@@ -977,10 +1026,11 @@ bool jit_lookup_cached(const std::vector<const OshmProgram*>& progs, std::vector
     return true;
 }
 
-void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, int* err, cudaStream_t st) {
+void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, int* err, cudaStream_t st,
+                void* copy) {
     const uint64_t slots = uint64_t(ctx().sm_count) * k.blocks_per_sm;
     const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
-    void* args[] = {&state, &ntiles, &err};
+    void* args[] = {&state, &ntiles, &err, &copy};
     HQ_CHECK_CUDA(cudaLaunchKernel((const void*)k.kern, dim3(grid), dim3(k.threads), args, k.smem, st));
 }
 

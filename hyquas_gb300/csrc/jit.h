@@ -27,7 +27,11 @@ std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>&
 // (nothing is compiled).
 bool jit_lookup_cached(const std::vector<const OshmProgram*>& progs, std::vector<JitKernel>& out);
 // `err`: the device error word (a RING kernel records a timed-out wait there)
-void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, int* err, cudaStream_t st);
+// `copy`, when not null, is a device-accessible host buffer that receives the
+// group's output as well (the last group of a run that leaves the final state
+// on the host)
+void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, int* err, cudaStream_t st,
+                void* copy = nullptr);
 std::string jit_source(const OshmProgram& prog);
 
 }  // namespace hq

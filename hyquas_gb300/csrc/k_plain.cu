@@ -303,8 +303,16 @@ struct PermuteParams {
     uint64_t dst_lo[32], dst_mid[32], dst_hi[8];
     uint16_t wr_lo[32], wr_mid[32], wr_hi[8];
     uint16_t swz_mid[32], swz_hi[8];
+    // write-order index w -> destination offset / smem read slot, composed
+    // (the destination of local index wr(w), the slot of wr(w)); both are
+    // bit-linear in w, so three tables per map
+    uint64_t wdst_lo[32], wdst_mid[32], wdst_hi[8];
+    uint16_t wslot_lo[32], wslot_mid[32], wslot_hi[8];
     uint8_t rest[64];   // tile-index bit r -> its (unmoved) physical bit
     int nrest;
+    // the tile index's bits as runs: (u >> run_src) & (2^run_len - 1) lands at run_dst
+    uint8_t run_src[32], run_dst[32], run_len[32];
+    int nruns;
     int pair_read;      // write-order bit 0 is local bit 0: index pairs are slot pairs
     int tile_bits;
     uint64_t ntiles;
@@ -343,35 +351,41 @@ __global__ void __launch_bounds__(256) k_permute_tile(float2* __restrict__ a,
     constexpr int PP = (1 << K) / 512;  // index pairs per thread
     extern __shared__ float2 tile[];
     const int t = threadIdx.x;
-    auto src = [&](int e) { return p.src_lo[e & 31] + p.src_mid[(e >> 5) & 31] + p.src_hi[e >> 10]; };
-    auto dst = [&](int j) { return p.dst_lo[j & 31] + p.dst_mid[(j >> 5) & 31] + p.dst_hi[j >> 10]; };
-    auto slot = [&](int j) { return j ^ p.swz_mid[(j >> 5) & 31] ^ p.swz_hi[j >> 10]; };
+    // Thread t moves index pairs e = 2t + 512m (m < PP) on both sides.  The
+    // maps are bit-linear, so their per-thread parts (index bits 0-9, the
+    // same for every tile) are looked up once here; bits 10-12 come from m
+    // and read the same table entry in every lane.
+    const int lo = (2 * t) & 31, mid = (2 * t) >> 5;
+    const uint64_t src0 = p.src_lo[lo] + p.src_mid[mid], src1 = p.src_lo[lo] + p.src_mid[mid + 16];
+    const uint64_t dst0 = p.wdst_lo[lo] + p.wdst_mid[mid], dst1 = p.wdst_lo[lo] + p.wdst_mid[mid + 16];
+    const unsigned st0 = (2 * t) ^ p.swz_mid[mid], st1 = (2 * t) ^ p.swz_mid[mid + 16];
+    const unsigned rd0 = p.wslot_lo[lo] ^ p.wslot_mid[mid], rd1 = p.wslot_lo[lo] ^ p.wslot_mid[mid + 16];
+    const unsigned rd_pair = p.wslot_lo[1];  // slot of write index w + 1 relative to w
     for (uint64_t u = blockIdx.x; u < p.ntiles; u += gridDim.x) {
         uint64_t base = 0;
-        for (int r = 0; r < p.nrest; r++) base |= ((u >> r) & 1) << p.rest[r];
+        for (int r = 0; r < p.nruns; r++)
+            base |= ((u >> p.run_src[r]) & ((uint64_t(1) << p.run_len[r]) - 1)) << p.run_dst[r];
         float4 v[PP];
 #pragma unroll
         for (int m = 0; m < PP; m++)
-            v[m] = __ldcs(reinterpret_cast<const float4*>(a + base + src(2 * (t + 256 * m))));
+            v[m] = __ldcs(reinterpret_cast<const float4*>(a + base + ((m & 1) ? src1 : src0) + p.src_hi[m >> 1]));
         // the swizzle leaves slot bit 0 alone: index pair (e, e + 1) is slot pair
         // (slot(e), slot(e) + 1), one 16-byte store
 #pragma unroll
         for (int m = 0; m < PP; m++)
-            *reinterpret_cast<float4*>(tile + slot(2 * (t + 256 * m))) = v[m];
+            *reinterpret_cast<float4*>(tile + (((m & 1) ? st1 : st0) ^ (512u * m) ^ p.swz_hi[m >> 1])) = v[m];
         __syncthreads();
 #pragma unroll
         for (int m = 0; m < PP; m++) {
-            const int w = 2 * (t + 256 * m);
-            const int j0 = p.wr_lo[w & 31] | p.wr_mid[(w >> 5) & 31] | p.wr_hi[w >> 10];
+            const unsigned r0 = ((m & 1) ? rd1 : rd0) ^ p.wslot_hi[m >> 1];
             float4 x;
             if (p.pair_read) {
-                x = *reinterpret_cast<const float4*>(tile + slot(j0));
+                x = *reinterpret_cast<const float4*>(tile + r0);
             } else {
-                const int j1 = p.wr_lo[(w + 1) & 31] | p.wr_mid[(w >> 5) & 31] | p.wr_hi[w >> 10];
-                const float2 x0 = tile[slot(j0)], x1 = tile[slot(j1)];
+                const float2 x0 = tile[r0], x1 = tile[r0 ^ rd_pair];
                 x = make_float4(x0.x, x0.y, x1.x, x1.y);
             }
-            __stcs(reinterpret_cast<float4*>(a + base + dst(j0)), x);
+            __stcs(reinterpret_cast<float4*>(a + base + ((m & 1) ? dst1 : dst0) + p.wdst_hi[m >> 1]), x);
         }
         __syncthreads();
     }
@@ -466,10 +480,42 @@ PermuteParams make_permute_params(int n, const int* dest_of) {
     for (int m = 0; m < 8; m++)
         for (int b = 0; b < 3; b++)
             if (((m >> b) & 1) && 10 + b < K) p.swz_hi[m] ^= uint16_t(1) << target[10 + b];
+    // composed write-side maps, one entry per write-order bit
+    uint64_t wd[kPermuteMaxTileBits];
+    uint16_t ws[kPermuteMaxTileBits];
+    for (int b = 0; b < K; b++) {
+        const int j = wbit[b];  // local bit written at write-order bit b
+        wd[b] = uint64_t(1) << dest_of[loc_src[j]];
+        uint16_t sl = uint16_t(1u << j);
+        if (j >= 5 && j < 10) sl ^= p.swz_mid[1 << (j - 5)];
+        if (j >= 10) sl ^= p.swz_hi[1 << (j - 10)];
+        ws[b] = sl;
+    }
+    auto fillc = [&](uint64_t* d, uint16_t* sl, int nent, int first) {
+        for (int w = 0; w < nent; w++)
+            for (int b = 0; (1 << b) <= w; b++)
+                if (((w >> b) & 1) && first + b < K) {
+                    d[w] += wd[first + b];
+                    sl[w] ^= ws[first + b];
+                }
+    };
+    fillc(p.wdst_lo, p.wslot_lo, 32, 0);
+    fillc(p.wdst_mid, p.wslot_mid, 32, 5);
+    fillc(p.wdst_hi, p.wslot_hi, 8, 10);
     p.tile_bits = K;
     p.nrest = 0;
     for (int b = 0; b < n; b++)
         if (!((used >> b) & 1)) p.rest[p.nrest++] = (uint8_t)b;
+    p.nruns = 0;
+    for (int r = 0; r < p.nrest;) {
+        int len = 1;
+        while (r + len < p.nrest && p.rest[r + len] == p.rest[r] + len) len++;
+        p.run_src[p.nruns] = (uint8_t)r;
+        p.run_dst[p.nruns] = p.rest[r];
+        p.run_len[p.nruns] = (uint8_t)len;
+        p.nruns++;
+        r += len;
+    }
     p.ntiles = uint64_t(1) << (n - K);
     return p;
 }

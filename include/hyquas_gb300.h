@@ -277,6 +277,16 @@ hq_status hq_circuit_program_bytes(hq_circuit c, uint64_t* bytes);
  * Circuit::run, src/circuit.cpp:16-71; elapsed_us = device time of the run
  * (the reference's "Time Cost"). */
 hq_status hq_circuit_run(hq_circuit c, hq_state s, double* elapsed_us);
+/* Run the compiled schedule on s and leave the final state in logical order
+ * at host_amps (2 * 2^n floats, interleaved re/im): the reference's run
+ * followed by its full-state readback into Circuit::result
+ * (src/circuit.cpp:46-62, kernelDeviceToHost).  With a pinned buffer
+ * (hq_host_alloc) and a schedule whose last group runs a generated kernel
+ * and ends in the canonical layout, that group writes each finished amplitude
+ * to HBM and to host_amps in the same pass; otherwise the run is followed by
+ * a copy.  s holds the final state afterwards either way.  elapsed_us =
+ * device time of run and readback. */
+hq_status hq_circuit_run_to_host(hq_circuit c, hq_state s, float* host_amps, double* elapsed_us);
 /* Run the compiled schedule on s with a CUDA event pair around every group;
  * group_us[g] = device time of group g (num_groups entries).  The reference's
  * MEASURE_STAGE per-group timing, src/executor.cpp:406-458. */

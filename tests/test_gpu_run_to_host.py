@@ -1,0 +1,76 @@
+"""hq_circuit_run_to_host: a run followed by the full-state readback of the
+reference's Circuit::run + result (src/circuit.cpp:46-62).  The fused form
+(the last group writes HBM and the pinned host buffer in one pass) must give
+exactly the bytes of run + store; the copy form covers unpinned buffers and
+runs that end outside the canonical layout."""
+import numpy as np
+import pytest
+
+from hyquas_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _compiled(hq, n, desc):
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile("oshm", specialize=1)  # generated kernels for every group
+    return c
+
+
+def _run_and_store(hq, c, n):
+    s = hq.State(n)
+    s.init_zero()
+    c.run_on(s)
+    return s.store()
+
+
+def test_fused_readback_is_run_then_store(hq, oracle):
+    n = 24  # 128 MiB: the huge-page pinned buffer path
+    desc = W.grid_random(5, 2, 12, 6)
+    c = _compiled(hq, n, desc)
+    ref = _run_and_store(hq, c, n)
+    buf = hq.PinnedBuffer(1 << n)
+    buf.array[:] = np.complex64(complex(np.nan, np.nan))
+    s = hq.State(n)
+    s.init_zero()
+    us = c.run_to_host(s, buf.array)
+    assert us > 0
+    assert np.array_equal(buf.array, ref)  # every amplitude written, bit for bit
+    assert np.array_equal(s.store(), ref)  # and the device state holds the same
+    cmp = oracle.compare(oracle.run_f64(n, desc), buf.array)
+    assert cmp["max_abs_err"] <= 1e-5 and cmp["one_minus_fidelity"] <= 1e-6, cmp
+
+
+def test_unpinned_buffer_takes_the_copy(hq):
+    n = 20
+    desc = W.grid_random(6, 4, 5, 5)
+    c = _compiled(hq, n, desc)
+    ref = _run_and_store(hq, c, n)
+    out = np.full(1 << n, np.nan, dtype=np.complex64)
+    s = hq.State(n)
+    s.init_zero()
+    c.run_to_host(s, out)
+    assert np.array_equal(out, ref)
+
+
+def test_run_ending_in_a_swapped_layout_reads_back_logical_order(hq, oracle):
+    n = 18
+    desc = W.grid_random(7, 3, 6, 4) + [(W.SWAP, 0, 17, -1, ()), (W.SWAP, 3, 12, -1, ())]
+    c = _compiled(hq, n, desc)
+    buf = hq.PinnedBuffer(1 << n)
+    s = hq.State(n)
+    s.init_zero()
+    c.run_to_host(s, buf.array)
+    cmp = oracle.compare(oracle.run_f64(n, desc), buf.array)
+    assert cmp["max_abs_err"] <= 1e-5 and cmp["one_minus_fidelity"] <= 1e-6, cmp
+    assert np.array_equal(s.store(), buf.array)
+
+
+def test_run_to_host_rejects_a_wrong_buffer(hq):
+    n = 10
+    c = _compiled(hq, n, W.grid_random(8, 2, 5, 2))
+    s = hq.State(n)
+    s.init_zero()
+    with pytest.raises(ValueError):
+        c.run_to_host(s, np.zeros(1 << (n - 1), dtype=np.complex64))
