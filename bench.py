@@ -311,22 +311,25 @@ def run_ours(args, dist: Dist):
 
     # e2e through the public API with host buffers: per step compile, run from
     # |0..0> and read the whole state back into pinned host memory, as the
-    # reference's Circuit::run + result does (src/circuit.cpp:46-62).
-    # Circuit.run_to_host writes the final state to HBM and to the pinned
-    # buffer in the last group's pass, so the readback is not a separate copy.
+    # reference's Circuit::run + result does (src/circuit.cpp:46-62).  Two
+    # states alternate: step k's readback (State.store_async: a copy kernel on
+    # a few SMs) runs beside step k+1's compile and run on the other SMs; the
+    # region ends when the last readback has landed.
     e2e = None
     if not args.no_e2e:
-        pinned = hq.PinnedBuffer(1 << n)
-        # the host link's rate, and the first transfer into the fresh pinned
-        # pages out of the timed region
+        states = [state, hq.State(n)]
+        pinned = [hq.PinnedBuffer(1 << n), hq.PinnedBuffer(1 << n)]
+        # the host link's rate, and the first transfer into each buffer's fresh
+        # pinned pages, out of the timed region
         tr = time.perf_counter()
-        state.store(pinned.array)
+        states[1].store(pinned[1].array)
         readback_gbs = 8.0 * (1 << n) / (time.perf_counter() - tr) / 1e9
+        states[0].store(pinned[0].array)
         h2d = 0
-        parts = []  # per step: compile, init + run + readback, release (ms)
-        dev_ms = []
+        parts = []  # per step: compile, init + run, queue readback + release (ms)
         t0 = time.perf_counter()
         for i in range(args.steps):
+            st = states[i % 2]
             ta = time.perf_counter()
             c2 = hq.Circuit(n)
             c2.addGates(gates)
@@ -334,19 +337,37 @@ def run_ours(args, dist: Dist):
                        tile_qubits=args.tile_qubits, coalesce=args.coalesce)
             h2d = c2.program_bytes()
             tb = time.perf_counter()
-            state.init_zero()
-            dev_ms.append(c2.run_to_host(state, pinned.array) / 1e3)
+            st.init_zero()
+            c2.run_on(st)
             tc = time.perf_counter()
+            st.store_async(pinned[i % 2].array)
             del c2
             parts.append([round((tb - ta) * 1e3, 1), round((tc - tb) * 1e3, 1),
                           round((time.perf_counter() - tc) * 1e3, 1)])
+        for s_ in states:
+            s_.wait()
         e2e_s = dist.max(time.perf_counter() - t0)
+        # the same steps without overlap: run_to_host writes the final state to
+        # HBM and to the pinned buffer in the last group's pass
+        seq_steps = max(1, min(args.steps, 5))
+        seq_ms = []
+        f0 = time.perf_counter()
+        for i in range(seq_steps):
+            c2 = hq.Circuit(n)
+            c2.addGates(gates)
+            c2.compile(backend=args.backend, specialize=args.specialize,
+                       tile_qubits=args.tile_qubits, coalesce=args.coalesce)
+            state.init_zero()
+            seq_ms.append(round(c2.run_to_host(state, pinned[0].array) / 1e3, 2))
+            del c2
+        seq_s = dist.max(time.perf_counter() - f0)
         # a new circuit every step (same shape, another seed): the compile
         # includes generating and compiling its group kernels
         fresh_steps = max(1, min(args.steps, 5))
         fresh_parts = []
         f0 = time.perf_counter()
         for i in range(fresh_steps):
+            st = states[i % 2]
             ta = time.perf_counter()
             c2 = hq.Circuit(n)
             c2.addGates(W.to_gates(W.grid_random(1000 + 97 * i + dist.rank, rows, cols, 20)))
@@ -355,30 +376,36 @@ def run_ours(args, dist: Dist):
             c2.compile(backend=args.backend, specialize=3 if args.specialize == 2 else args.specialize,
                        tile_qubits=args.tile_qubits, coalesce=args.coalesce)
             tb = time.perf_counter()
-            state.init_zero()
-            c2.run_to_host(state, pinned.array)
+            st.init_zero()
+            c2.run_on(st)
             tc = time.perf_counter()
+            st.store_async(pinned[i % 2].array)
             del c2
             fresh_parts.append([round((tb - ta) * 1e3, 1), round((tc - tb) * 1e3, 1)])
+        for s_ in states:
+            s_.wait()
         fresh_s = dist.max(time.perf_counter() - f0)
         e2e = {"value": dist.ws * args.steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(8 * (1 << n)),
-               "readback": "fused: the last group writes HBM and the pinned host buffer "
-                           "in one pass (Circuit.run_to_host)",
+               "readback": "State.store_async: a copy kernel on 8 SMs writes the pinned buffer "
+                           "while the next step runs on the other SMs; two states alternate",
                "readback_gbs": readback_gbs,
-               "pinned_numa_nodes": pinned.numa_nodes(),
-               "step_parts_ms": {"compile": [p[0] for p in parts], "init_run_readback": [p[1] for p in parts],
-                                 "release": [p[2] for p in parts],
-                                 "device_run_readback": [round(x, 2) for x in dev_ms]},
+               "pinned_numa_nodes": [b.numa_nodes() for b in pinned],
+               "step_parts_ms": {"compile": [p[0] for p in parts], "init_run": [p[1] for p in parts],
+                                 "queue_release": [p[2] for p in parts]},
+               "sequential_run_to_host": {"value": dist.ws * seq_steps / seq_s, "unit": UNIT,
+                                          "steps": seq_steps, "device_run_readback_ms": seq_ms},
                "fresh_circuit": {"value": dist.ws * fresh_steps / fresh_s, "unit": UNIT,
                                  "steps": fresh_steps,
                                  "compile_ms": [p[0] for p in fresh_parts],
-                                 "init_run_readback_ms": [p[1] for p in fresh_parts],
+                                 "init_run_ms": [p[1] for p in fresh_parts],
                                  "what": "a new seeded circuit of the same shape every step: "
                                          "planning inside the step; its group kernels compile "
                                          "on a host thread (specialize=3) while the run uses "
                                          "the interpreter for groups not compiled yet"}}
-        pinned.free()
+        states[1].free()
+        for b in pinned:
+            b.free()
 
     # accuracy against the FP64 gate-by-gate oracle (outside the timed region):
     # one fresh run from |0..0>, the whole state read back
@@ -698,17 +725,27 @@ def run_batch(args, dist: Dist):
 
 
 def run_dense28(args, dist: Dist):
-    """The 20-qubit plain-path circuit family (U3 on every qubit, then CNOT on
-    a random matching, per layer) at 28 qubits: every single-qubit gate is a
-    general complex 2x2, the case where fused TransMM groups can beat
-    OShareMem.  OShareMem-only, TransMM-only and the hybrid choice, each
-    against the FP64 oracle."""
+    """Dense circuits at 28 qubits, OShareMem-only, TransMM-only and the hybrid
+    choice, each against the FP64 oracle.  dense28: the 20-qubit plain-path
+    family (U3 on every qubit, then CNOT on a random matching, per layer);
+    blocked28: deep U3+CNOT blocks of 7 qubits joined by single CNOTs, where
+    a block's layers fuse into one 7-qubit unitary (the reference's mix mode,
+    src/compiler.cpp:248-280)."""
     import hyquas_gb300 as hq
     from hyquas_gb300 import workloads as W
     import oracle as O
     hq.init(dist.local)
     n = args.dense_qubits
-    desc = W.plain_u3_cnot(1, n, args.dense_layers)
+    blocked = args.workload == "blocked28"
+    if blocked:
+        desc = W.blocked_u3_cnot(11, n, 7, args.dense_layers, 2)
+        what = (f"{n} qubits in blocks of 7, 2 rounds of {args.dense_layers} layers per block (U3 on "
+                "every qubit + CNOTs on alternating neighbour pairs inside the block, then one CNOT "
+                "joining neighbouring blocks), |0..0>")
+    else:
+        desc = W.plain_u3_cnot(1, n, args.dense_layers)
+        what = (f"{n} qubits, {args.dense_layers} layers of U3 on every qubit + CNOT on a random "
+                "matching, |0..0>")
     gates = W.to_gates(desc)
     ref = O.run_f64(n, desc)
     state = hq.State(n)
@@ -738,11 +775,10 @@ def run_dense28(args, dist: Dist):
     best = min(rows, key=lambda r: r["ms"])
     peak, peak_kind = measured_peaks()
     achieved = best["passes"] * 16.0 * (1 << n) / (best["ms"] * 1e-3) / 1e9
-    line = base_line(args, dist, f"{n}q U3+CNOT circuit time (ms), best backend", best["ms"], "ms",
-                     best["ms"], False,
-                     f"{n} qubits, {args.dense_layers} layers of U3 on every qubit + CNOT on a random "
-                     "matching, |0..0>; OShareMem-only, hybrid and TransMM-only (split BF16, 7-qubit "
-                     "groups), each checked against the FP64 oracle",
+    line = base_line(args, dist, f"{n}q {'blocked ' if blocked else ''}U3+CNOT circuit time (ms), "
+                     "best backend", best["ms"], "ms", best["ms"], False,
+                     what + "; OShareMem-only, hybrid and TransMM-only (split BF16, 7-qubit groups), "
+                     "each checked against the FP64 oracle",
                      {"cases": rows, "best_backend": best["backend"]})
     line.update({"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                               "frac": achieved / peak, "traffic": None,
@@ -962,7 +998,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP64 oracle comparison (grid30: about a minute of CPU)")
     ap.add_argument("--workload", default="grid30",
-                    choices=["grid30", "plain20", "qft28", "batch", "serve", "remap", "dense28"])
+                    choices=["grid30", "plain20", "qft28", "batch", "serve", "remap", "dense28",
+                             "blocked28"])
     ap.add_argument("--dense-qubits", type=int, default=28)
     ap.add_argument("--dense-layers", type=int, default=10)
     ap.add_argument("--remap-qubits", type=int, default=30)
@@ -985,7 +1022,8 @@ def main():
             run_ours(args, dist)
         else:
             {"plain20": run_plain20, "qft28": run_qft28, "batch": run_batch,
-             "serve": run_serve, "remap": run_remap, "dense28": run_dense28}[args.workload](args, dist)
+             "serve": run_serve, "remap": run_remap, "dense28": run_dense28,
+             "blocked28": run_dense28}[args.workload](args, dist)
     finally:
         dist.close()
 

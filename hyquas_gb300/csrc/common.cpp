@@ -103,6 +103,17 @@ void dev_free_ordered(void* p, size_t bytes) {
     c.in_use = c.in_use >= bytes ? c.in_use - bytes : 0;
 }
 
+int compute_sms() {
+    Context& c = ctx();
+    if (c.rb_sms > 0 && c.rb_done) {
+        const cudaError_t q = cudaEventQuery(c.rb_done);
+        if (q == cudaErrorNotReady) return c.sm_count - c.rb_sms;
+        HQ_CHECK_CUDA(q);
+        c.rb_sms = 0;
+    }
+    return c.sm_count;
+}
+
 void check_device_error() {
     Context& c = ctx();
     // read into page-locked memory: a pageable destination would make this a

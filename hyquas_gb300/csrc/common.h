@@ -54,6 +54,11 @@ struct Context {
     size_t partials_cap = 0;       // doubles
     double* h_pinned = nullptr;    // pinned readback of reductions
     size_t pinned_cap = 0;
+    // SM-driven readbacks to pinned host memory run on a few SMs of their
+    // own; while the latest is in flight, the persistent group kernels launch
+    // on the others so that none of their blocks waits for an SM
+    cudaEvent_t rb_done = nullptr;
+    int rb_sms = 0;
 };
 
 Context& ctx();               // initialises on first use (device 0 unless hq_init chose)
@@ -66,6 +71,7 @@ void dev_free(void* p, size_t bytes);
 void* dev_alloc_ordered(size_t bytes);
 void dev_free_ordered(void* p, size_t bytes);
 void check_device_error();      // reads and clears the device error word
+int compute_sms();               // SMs a persistent kernel may fill now
 
 inline int popcount64(uint64_t x) { return __builtin_popcountll(x); }
 inline int ctz64(uint64_t x) { return __builtin_ctzll(x); }

@@ -162,6 +162,9 @@ void launch_bit_swap(void* state, int n, int a, int b, void* stream);
 constexpr int kPermuteMaxTileBits = 13;
 int permute_tile_bits(int n, const int* dest_of);
 void launch_permute_bits(void* state, int n, const int* dest_of, void* stream);
+// bytes from device memory d to a device-mapped pinned host buffer, by `ctas`
+// blocks (a few SMs); stream-ordered
+void launch_readback(const void* d, void* host_mapped, uint64_t bytes, int ctas, void* stream);
 void launch_oshm(const OshmLaunch& p, void* stream);
 int oshm_threads(int k, int r);
 int oshm_reg_bits(int k);

@@ -104,10 +104,12 @@ DI unsigned swz(unsigned x) { unsigned f = ((x >> 4) ^ (x >> 7) ^ (x >> 10) ^ (x
 DI void cpa16(unsigned s, const void* g) { asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(g) : "memory"); }
 DI float F(unsigned b) { return __int_as_float((int)b); }
 // a finished amplitude pair to the state and, when the run also leaves a copy
-// of the final state in (device-mapped) host memory, to that copy
-DI void st_amps(float2* state, float2* copy, u64 idx, float4 w) {
+// of the final state in (device-mapped) host memory, to that copy; the
+// kernel's stores are emitted twice, under one test of `copy`, so that the
+// common form is plain stores
+template <bool C> DI void st_amps(float2* state, float2* copy, u64 idx, float4 w) {
     *(float4*)(state + idx) = w;
-    if (copy) *(float4*)(copy + idx) = w;
+    if (C) *(float4*)(copy + idx) = w;
 }
 // Bounded wait for phase `par` of the mbarrier at `addr`, decided by the whole
 // group (barrier `gbar`, `cnt` threads): either every thread of the group saw
@@ -797,14 +799,17 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
         }
         if (lastp) {
             // vector j holds the amplitudes at pidx | (its register bits) and + 1
-            for (int j = 0; j < NV; j++) {
-                uint64_t off = 0;
-                for (int b = 1; b < R; b++)
-                    if ((j >> (b - 1)) & 1) off |= uint64_t(1) << tile_phys[P.r_local[b]];
-                o << "{ float4 w; vunpack(r" << j << ", w.x, w.z); vunpack(i" << j
-                  << ", w.y, w.w); st_amps(state, copy, pidx | " << hex64(off) << ", w); }\n";
+            for (int form = 0; form < 2; form++) {
+                o << (form == 0 ? "if (copy == nullptr) {\n" : "} else {\n");
+                for (int j = 0; j < NV; j++) {
+                    uint64_t off = 0;
+                    for (int b = 1; b < R; b++)
+                        if ((j >> (b - 1)) & 1) off |= uint64_t(1) << tile_phys[P.r_local[b]];
+                    o << "{ float4 w; vunpack(r" << j << ", w.x, w.z); vunpack(i" << j << ", w.y, w.w); st_amps<"
+                      << (form ? "true" : "false") << ">(state, copy, pidx | " << hex64(off) << ", w); }\n";
+                }
             }
-            o << "}\n";
+            o << "}\n}\n";
             continue;
         }
         for (int j = 0; j < NV; j++) {
@@ -825,16 +830,20 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
         // staged write-back; pieces are (re0, re1, im0, im1) after a phase and
         // as loaded when there is none
         o << "const u64 gdst = base + toff;\n";
-        for (int m = 0; m < PPT; m++) {
-            if (prog.phases.empty())
-                o << "st_amps(state, copy, gdst + " << hex64(poff[m]) << ", buf[(tslot ^ " << pslot[m]
-                  << "u) >> 1]);\n";
-            else
-                o << "{ const ulonglong2 q = ((const ulonglong2*)buf)[(tslot ^ " << pslot[m]
-                  << "u) >> 1]; float4 w; vunpack(q.x, w.x, w.z); vunpack(q.y, w.y, w.w); "
-                     "st_amps(state, copy, gdst + "
-                  << hex64(poff[m]) << ", w); }\n";
+        for (int form = 0; form < 2; form++) {
+            const char* tf = form ? "true" : "false";
+            o << (form == 0 ? "if (copy == nullptr) {\n" : "} else {\n");
+            for (int m = 0; m < PPT; m++) {
+                if (prog.phases.empty())
+                    o << "st_amps<" << tf << ">(state, copy, gdst + " << hex64(poff[m]) << ", buf[(tslot ^ "
+                      << pslot[m] << "u) >> 1]);\n";
+                else
+                    o << "{ const ulonglong2 q = ((const ulonglong2*)buf)[(tslot ^ " << pslot[m]
+                      << "u) >> 1]; float4 w; vunpack(q.x, w.x, w.z); vunpack(q.y, w.y, w.w); st_amps<" << tf
+                      << ">(state, copy, gdst + " << hex64(poff[m]) << ", w); }\n";
+            }
         }
+        o << "}\n";
         o << SYNC;
         if (ring) o << "if (tile_of(i + 3) < ntiles) load_tile(tile_of(i + 3), bi, i + 3);\n";
     }
@@ -1028,7 +1037,7 @@ bool jit_lookup_cached(const std::vector<const OshmProgram*>& progs, std::vector
 
 void jit_launch(const JitKernel& k, void* state, uint64_t ntiles, int* err, cudaStream_t st,
                 void* copy) {
-    const uint64_t slots = uint64_t(ctx().sm_count) * k.blocks_per_sm;
+    const uint64_t slots = uint64_t(compute_sms()) * k.blocks_per_sm;
     const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
     void* args[] = {&state, &ntiles, &err, &copy};
     HQ_CHECK_CUDA(cudaLaunchKernel((const void*)k.kern, dim3(grid), dim3(k.threads), args, k.smem, st));

@@ -735,7 +735,7 @@ void launch_k(const OshmLaunch& p, cudaStream_t s) {
         HQ_REQUIRE(blocks_per_sm >= 1, HQ_ERR_UNSUPPORTED, "oshm<%d>: does not fit on an SM", K);
     }
     HQ_REQUIRE(p.ntiles >= 1, HQ_ERR_INVALID, "oshm: no tiles");
-    const uint64_t slots = uint64_t(ctx().sm_count) * blocks_per_sm;
+    const uint64_t slots = uint64_t(compute_sms()) * blocks_per_sm;
     const unsigned grid = (unsigned)(p.ntiles < slots ? p.ntiles : slots);
     k_oshm<K, R><<<grid, T, smem, s>>>(p);
     HQ_CHECK_CUDA(cudaGetLastError());

@@ -391,6 +391,30 @@ __global__ void __launch_bounds__(256) k_permute_tile(float2* __restrict__ a,
     }
 }
 
+// Device -> pinned host copy run by a few SMs: 16-byte streaming loads from
+// HBM and plain stores through the host mapping, four per thread in flight.
+__global__ void __launch_bounds__(512) k_readback(const float4* __restrict__ src,
+                                                  float4* __restrict__ dst, uint64_t n4) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+        const float4 a = __ldcs(src + i), b = __ldcs(src + i + stride), c = __ldcs(src + i + 2 * stride),
+                     d = __ldcs(src + i + 3 * stride);
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < n4; i += stride) dst[i] = __ldcs(src + i);
+}
+
+void launch_readback(const void* d, void* host_mapped, uint64_t bytes, int ctas, void* stream) {
+    HQ_REQUIRE(bytes % 16 == 0 && ((uintptr_t)d % 16) == 0 && ((uintptr_t)host_mapped % 16) == 0,
+               HQ_ERR_INVALID, "readback: 16-byte aligned buffers and size");
+    k_readback<<<ctas, 512, 0, (cudaStream_t)stream>>>((const float4*)d, (float4*)host_mapped, bytes / 16);
+    HQ_CHECK_CUDA(cudaGetLastError());
+}
+
 int permute_tile_bits(int n, const int* dest_of) {
     uint64_t t = 0;
     for (int b = 0; b < n && b < 5; b++) t |= uint64_t(1) << b;

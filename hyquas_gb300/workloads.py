@@ -73,6 +73,28 @@ def plain_u3_cnot(seed: int = 1, n: int = 20, layers: int = 10):
     return gates
 
 
+def blocked_u3_cnot(seed: int = 11, n: int = 28, block: int = 7, depth: int = 20, rounds: int = 2):
+    """A modular circuit: the qubits form blocks of `block` neighbours; per round every block
+    runs `depth` layers of U3 on each of its qubits and CNOTs on alternating neighbour pairs
+    inside the block, then one CNOT joins each block to the next.  Deep dense blocks are the
+    case the reference's mix mode fuses into one unitary per block (src/compiler.cpp:248-280)."""
+    rng = SplitMix64(seed)
+    gates = []
+    nb = n // block
+    for _ in range(rounds):
+        for b in range(nb):
+            q0 = b * block
+            for d in range(depth):
+                for q in range(q0, q0 + block):
+                    gates.append(g1(U3, q, rng.uniform() * TWO_PI, rng.uniform() * TWO_PI,
+                                    rng.uniform() * TWO_PI))
+                for q in range(q0 + (d & 1), q0 + block - 1, 2):
+                    gates.append(g2(CNOT, q, q + 1))
+        for b in range(nb - 1):
+            gates.append(g2(CNOT, b * block + block - 1, (b + 1) * block))
+    return gates
+
+
 def grid_couplers(rows: int, cols: int):
     """The 4 alternating coupler patterns of a rows x cols grid: horizontal
     couplers with even / odd column, vertical couplers with even / odd row."""

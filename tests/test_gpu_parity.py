@@ -582,3 +582,20 @@ def test_max_size_34_qubits(hq, oracle):
     amp0 = s.amps(np.array([0], dtype=np.uint64))[0]
     assert abs(abs(amp0) ** 2 - 1.0) < 1e-4
     s.free()
+
+
+def test_blocked_circuit_hybrid_takes_transmm(hq, oracle):
+    """Deep dense 7-qubit blocks: the hybrid partitioner fuses blocks into
+    TransMM groups (the reference's mix mode, src/compiler.cpp:248-280) and the
+    mixed schedule matches the FP64 oracle."""
+    n = 21
+    desc = W.blocked_u3_cnot(11, n, 7, 10, 2)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile("hybrid")
+    kinds = [b for (b, _, _, _) in c.schedule()]
+    assert hq.BACKEND_TRANSMM in kinds and hq.BACKEND_OSHM in kinds, kinds
+    s = hq.State(n)
+    s.init_zero()
+    c.run_on(s)
+    check(oracle, oracle.run_f64(n, desc), s.store())

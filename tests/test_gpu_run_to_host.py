@@ -74,3 +74,25 @@ def test_run_to_host_rejects_a_wrong_buffer(hq):
     s.init_zero()
     with pytest.raises(ValueError):
         c.run_to_host(s, np.zeros(1 << (n - 1), dtype=np.complex64))
+
+
+def test_async_readback_beside_the_next_run(hq):
+    """State.store_async into a large pinned buffer runs as a copy kernel on a
+    few SMs; a circuit run on another state meanwhile launches its persistent
+    kernels on the other SMs.  Both results are exact."""
+    n = 24
+    ca = _compiled(hq, n, W.grid_random(9, 2, 12, 5))
+    cb = _compiled(hq, n, W.grid_random(10, 2, 12, 5))
+    ref_a = _run_and_store(hq, ca, n)
+    ref_b = _run_and_store(hq, cb, n)
+    sa, sb = hq.State(n), hq.State(n)
+    buf = hq.PinnedBuffer(1 << n)
+    buf.array[:] = np.complex64(complex(np.nan, np.nan))
+    sa.init_zero()
+    ca.run_on(sa)
+    sa.store_async(buf.array)
+    sb.init_zero()
+    cb.run_on(sb)
+    sa.wait()
+    assert np.array_equal(buf.array, ref_a)
+    assert np.array_equal(sb.store(), ref_b)
