@@ -1,4 +1,5 @@
 #include "common.h"
+#include "device.h"
 
 #include <cstdarg>
 #include <cstdio>
@@ -42,7 +43,8 @@ static void init_device(int device) {
     HQ_CHECK_CUDA(cudaMalloc(&c.d_partials, sizeof(double) * c.partials_cap));
     c.pinned_cap = 1 << 16;
     HQ_CHECK_CUDA(cudaMallocHost(&c.h_pinned, sizeof(double) * c.pinned_cap));
-    HQ_CHECK_CUDA(cudaMallocHost(&c.h_error, sizeof(int) * 4));
+    HQ_CHECK_CUDA(cudaHostAlloc(&c.h_error, sizeof(int) * 4, cudaHostAllocMapped));
+    HQ_CHECK_CUDA(cudaHostGetDevicePointer((void**)&c.h_error_dev, c.h_error, 0));
 }
 
 Context& ctx() {
@@ -116,13 +118,13 @@ int compute_sms() {
 
 void check_device_error() {
     Context& c = ctx();
-    // read into page-locked memory: a pageable destination would make this a
-    // staged, host-synchronous copy behind whatever else the copy engines hold
-    HQ_CHECK_CUDA(cudaMemcpyAsync(c.h_error, c.d_error, sizeof(int) * 4, cudaMemcpyDeviceToHost,
-                                  c.stream));
+    // a one-thread kernel writes the word into mapped page-locked memory: no
+    // copy-engine transfer, which on GB300 can wait tens of milliseconds
+    // behind a large readback in flight to the same host
+    launch_error_readout(c.d_error, c.h_error_dev, c.stream);
     HQ_CHECK_CUDA(cudaStreamSynchronize(c.stream));
     int h[4];
-    for (int i = 0; i < 4; i++) h[i] = c.h_error[i];
+    for (int i = 0; i < 4; i++) h[i] = reinterpret_cast<volatile int*>(c.h_error)[i];
     if (h[0] != 0) {
         HQ_CHECK_CUDA(cudaMemsetAsync(c.d_error, 0, sizeof(int) * 4, c.stream));
         HQ_CHECK_CUDA(cudaStreamSynchronize(c.stream));

@@ -49,7 +49,8 @@ struct Context {
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // asynchronous readbacks (made on first use)
     int* d_error = nullptr;        // device error word (bounded waits, bad indices)
-    int* h_error = nullptr;        // its page-locked host copy
+    int* h_error = nullptr;        // its page-locked, device-mapped host copy
+    int* h_error_dev = nullptr;    // h_error's device address
     double* d_partials = nullptr;  // reduction partials (FP64), see k_plain.cu
     size_t partials_cap = 0;       // doubles
     double* h_pinned = nullptr;    // pinned readback of reductions

@@ -309,10 +309,31 @@ double predicted_time(int n, const std::vector<hq_gate>& gates, const Partition&
 // 13, 69.9 at 12, 67.2 at 11; QFT-28 5.1 ms at 13).  The reference reads
 // per-qubit-count parameter files for its choices instead
 // (src/evaluator.cpp:60-109).
+//
+// The hybrid's per-group choice (the reference's, by predicted time per gate)
+// can miss a schedule that is faster as a whole: deep dense blocks that all
+// fuse into TransMM groups, say.  So the hybrid also partitions the circuit
+// OShareMem-only and TransMM-only and keeps whichever of the three the cost
+// model predicts fastest.
 Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<int>& pos0,
                     const CompileConfig& cfg) {
-    if (!cfg.tile_auto || cfg.reference || cfg.backend == HQ_BACKEND_TRANSMM)
-        return partition_width(n, gates, pos0, cfg);
+    auto one = [&](const CompileConfig& c) {
+        Partition p = partition_width(n, gates, pos0, c);
+        if (c.backend != HQ_BACKEND_HYBRID || c.reference) return p;
+        double bt = predicted_time(n, gates, p, c);
+        for (int alt : {HQ_BACKEND_OSHM, HQ_BACKEND_TRANSMM}) {
+            CompileConfig a = c;
+            a.backend = alt;
+            Partition q = partition_width(n, gates, pos0, a);
+            const double qt = predicted_time(n, gates, q, a);
+            if (qt < bt) {
+                p = std::move(q);
+                bt = qt;
+            }
+        }
+        return p;
+    };
+    if (!cfg.tile_auto || cfg.reference || cfg.backend == HQ_BACKEND_TRANSMM) return one(cfg);
     Partition best;
     double best_t = 0;
     bool have = false;
@@ -320,7 +341,7 @@ Partition partition(int n, const std::vector<hq_gate>& gates, const std::vector<
         if (t > n && have) continue;
         CompileConfig c = cfg;
         c.tile = std::min(t, n);
-        Partition p = partition_width(n, gates, pos0, c);
+        Partition p = one(c);
         const double pt = predicted_time(n, gates, p, c);
         if (!have || pt < best_t * 0.85) {
             best = std::move(p);
@@ -548,13 +569,6 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
     int pending_count = 0;
     std::vector<char> done(gates.size(), 0);
     size_t ndone = 0;
-    // Thread-index bits 5 and up select the warp.  While a phase keeps the
-    // previous phase's warp bits, every warp exchanges amplitudes only with
-    // itself and the generated kernel syncs the warp instead of the tile's
-    // threads; the planner keeps them where it can.
-    const int G = k - r;
-    const int nwarp = G > 5 ? G - 5 : 0;
-    std::vector<int> warp_bits;  // local tile bits at thread bits 5.., last phase
     while (ndone < gates.size()) {
         // register qubits of this phase: local qubit 0 always (the f32x2 lane),
         // plus up to r-1 targets chosen greedily in gate order
@@ -591,17 +605,10 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
                 if (diag[i] && loc[gates[i].target] >= 0) score[loc[gates[i].target]]++;
             // ties go to the highest tile qubits: the low ones stay thread bits, where
             // they give whole 32-byte sectors to the stores of neighbouring threads
-            // among equals, the previous phase's warp bits are taken last
-            auto is_warp = [&](int b) {
-                return std::find(warp_bits.begin(), warp_bits.end(), b) != warp_bits.end();
-            };
             std::vector<int> cand;
             for (int b = k - 1; b >= 1; b--)
                 if (!((rset >> b) & 1)) cand.push_back(b);
-            std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) {
-                if (score[a] != score[b]) return score[a] < score[b];
-                return !is_warp(a) && is_warp(b);
-            });
+            std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) { return score[a] < score[b]; });
             for (int b : cand) {
                 if (__builtin_popcount(rset) >= r) break;
                 rset |= 1u << b;
@@ -625,60 +632,7 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
         std::vector<int> gfree;
         for (int b = 0; b < k; b++)
             if (!((rset >> b) & 1)) gfree.push_back(b);
-        auto classes_left = [&](const std::vector<int>& w) {
-            for (int cls = 1; cls <= 3; cls++) {
-                bool found = false;
-                for (int b : gfree)
-                    if (slot_class(b) == cls && std::find(w.begin(), w.end(), b) == w.end()) found = true;
-                if (!found) return false;
-            }
-            return true;
-        };
-        auto all_free = [&](const std::vector<int>& w) {
-            for (int b : w)
-                if (std::find(gfree.begin(), gfree.end(), b) == gfree.end()) return false;
-            return true;
-        };
-        // the warp bits: the previous phase's if they are all thread bits
-        // again, else the free tile bits whose next non-diagonal gate comes
-        // last (they can stay warp bits longest)
-        // The last phase keeps the plain order: its lanes then cover the
-        // lowest tile bits, which its direct stores to HBM coalesce over.
-        bool last_phase = true;
-        {
-            size_t nm = 0;
-            for (size_t i = 0; i < gates.size(); i++)
-                if (!done[i]) nm++;
-            last_phase = nm == members.size();
-        }
-        std::vector<int> wsel;
-        if (nwarp > 0 && !last_phase) {
-            if ((int)warp_bits.size() == nwarp && all_free(warp_bits) && classes_left(warp_bits)) {
-                wsel = warp_bits;
-            } else {
-                std::vector<size_t> next_use(k, gates.size());
-                for (size_t i = gates.size(); i-- > 0;)
-                    if (!done[i] && !diag[i] && !std::count(members.begin(), members.end(), (int)i))
-                        next_use[loc[gates[i].target]] = i;
-                // tile bits 1-4 stay lane bits (whole sectors for the stores)
-                std::vector<int> cand;
-                for (int b : gfree)
-                    if (b >= 5) cand.push_back(b);
-                std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) {
-                    if (next_use[a] != next_use[b]) return next_use[a] > next_use[b];
-                    return a > b;
-                });
-                for (int b : cand) {
-                    if ((int)wsel.size() == nwarp) break;
-                    std::vector<int> w = wsel;
-                    w.push_back(b);
-                    if (classes_left(w)) wsel = w;
-                }
-                if ((int)wsel.size() != nwarp) wsel.clear();  // plain order below
-            }
-        }
         std::vector<int> order;
-        for (int b : wsel) gfree.erase(std::find(gfree.begin(), gfree.end(), b));
         auto take_class = [&](int cls) {
             for (size_t i = 0; i < gfree.size(); i++)
                 if (slot_class(gfree[i]) == cls) {
@@ -691,8 +645,6 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
         take_class(2);
         take_class(3);
         for (int b : gfree) order.push_back(b);
-        for (int b : wsel) order.push_back(b);
-        warp_bits.assign(order.begin() + (G - nwarp), order.end());
         for (size_t j = 0; j < order.size(); j++) {
             ph.g_local[j] = (uint8_t)order[j];
             ph.g_phys[j] = (uint8_t)phys_of[order[j]];

@@ -248,43 +248,6 @@ struct Gen {
                 if ((k0 || k1) && pair_needs_align(kind, k0 && k1, has_cout)) align(j, j | (1 << (J - 1)));
             }
         }
-        // Sign flips under a run-time condition (CZ-like gates with a qubit
-        // outside the register set): a mask chosen by the condition and
-        // XORed in unconditionally, straight-line code that the compiler
-        // interleaves with the FMA-pipe arithmetic around it (a branch would
-        // keep the ALU work apart from it)
-        {
-            const bool dneg = kind == OP_DOUT && (op.flags & OPF_D0_ONE) && m[6] == -1.f && m[7] == 0.f &&
-                              op.creg != 0;
-            if ((kind == OP_NEGHI && has_cout) || dneg) {
-                std::string cond;
-                if (has_cout) cond = "(pidx & " + hex64(op.cout) + ") == " + hex64(op.cout);
-                if (dneg) cond += std::string(cond.empty() ? "" : " && ") + "(pidx & " + hex64(op.tout) + ") != 0ull";
-                o << "{ const u64 sg = (" << cond << ") ? 0x8000000080000000ull : 0ull;\n";
-                auto flip = [&](int j, bool k0, bool k1) {
-                    if (k0 && k1)
-                        o << R(j) << " ^= sg; " << I(j) << " ^= sg;\n";
-                    else if (k0 || k1) {
-                        const char* lm = k0 ? "0x80000000ull" : "0x8000000000000000ull";
-                        o << R(j) << " ^= sg & " << lm << "; " << I(j) << " ^= sg & " << lm << ";\n";
-                    }
-                };
-                for (int j = 0; j < nv; j++) {
-                    bool k0, k1;
-                    if (kind == OP_DOUT) {
-                        lanes(op.creg, j, k0, k1);
-                        flip(j, k0, k1);
-                    } else if (J == 0) {
-                        if ((uint32_t(2 * j) & op.creg) == op.creg) flip(j, false, true);
-                    } else if (!(j & (1 << (J - 1)))) {
-                        lanes(op.creg, j, k0, k1);
-                        flip(j | (1 << (J - 1)), k0, k1);
-                    }
-                }
-                o << "}\n";
-                return;
-            }
-        }
         if (has_cout) o << "if ((pidx & " << hex64(op.cout) << ") == " << hex64(op.cout) << ") {\n";
         o << "{\n";
         if (kind == OP_DOUT) {

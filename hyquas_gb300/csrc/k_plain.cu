@@ -391,6 +391,15 @@ __global__ void __launch_bounds__(256) k_permute_tile(float2* __restrict__ a,
     }
 }
 
+__global__ void k_error_readout(const int* __restrict__ d, int* __restrict__ h) {
+    if (threadIdx.x < 4) h[threadIdx.x] = d[threadIdx.x];
+}
+
+void launch_error_readout(const int* d_error, int* h_mapped, void* stream) {
+    k_error_readout<<<1, 32, 0, (cudaStream_t)stream>>>(d_error, h_mapped);
+    HQ_CHECK_CUDA(cudaGetLastError());
+}
+
 // Device -> pinned host copy run by a few SMs: 16-byte streaming loads from
 // HBM and plain stores through the host mapping, four per thread in flight.
 __global__ void __launch_bounds__(512) k_readback(const float4* __restrict__ src,
