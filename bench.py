@@ -326,7 +326,8 @@ def run_ours(args, dist: Dist):
         readback_gbs = 8.0 * (1 << n) / (time.perf_counter() - tr) / 1e9
         states[0].store(pinned[0].array)
         h2d = 0
-        parts = []  # per step: compile, init + run, queue readback + release (ms)
+        parts = []  # per step: compile, readback age when its state is reused, init, run (ms)
+        issued = [None, None]
         t0 = time.perf_counter()
         for i in range(args.steps):
             st = states[i % 2]
@@ -337,13 +338,20 @@ def run_ours(args, dist: Dist):
                        tile_qubits=args.tile_qubits, coalesce=args.coalesce)
             h2d = c2.program_bytes()
             tb = time.perf_counter()
+            age = 0.0
+            if issued[i % 2] is not None:  # the state's previous readback has landed
+                st.wait()
+                age = (time.perf_counter() - issued[i % 2]) * 1e3
+            tw = time.perf_counter()
             st.init_zero()
+            td = time.perf_counter()
             c2.run_on(st)
             tc = time.perf_counter()
             st.store_async(pinned[i % 2].array)
+            issued[i % 2] = time.perf_counter()
             del c2
-            parts.append([round((tb - ta) * 1e3, 1), round((tc - tb) * 1e3, 1),
-                          round((time.perf_counter() - tc) * 1e3, 1)])
+            parts.append([round((tb - ta) * 1e3, 1), round(age, 1), round((td - tw) * 1e3, 1),
+                          round((tc - td) * 1e3, 1)])
         for s_ in states:
             s_.wait()
         e2e_s = dist.max(time.perf_counter() - t0)
@@ -391,8 +399,9 @@ def run_ours(args, dist: Dist):
                            "while the next step runs on the other SMs; two states alternate",
                "readback_gbs": readback_gbs,
                "pinned_numa_nodes": [b.numa_nodes() for b in pinned],
-               "step_parts_ms": {"compile": [p[0] for p in parts], "init_run": [p[1] for p in parts],
-                                 "queue_release": [p[2] for p in parts]},
+               "step_parts_ms": {"compile": [p[0] for p in parts],
+                                 "readback_age_at_reuse": [p[1] for p in parts],
+                                 "init": [p[2] for p in parts], "run": [p[3] for p in parts]},
                "sequential_run_to_host": {"value": dist.ws * seq_steps / seq_s, "unit": UNIT,
                                           "steps": seq_steps, "device_run_readback_ms": seq_ms},
                "fresh_circuit": {"value": dist.ws * fresh_steps / fresh_s, "unit": UNIT,

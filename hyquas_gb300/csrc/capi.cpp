@@ -99,8 +99,17 @@ hq_status hq_host_alloc(uint64_t bytes, void** out) {
         void* p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
         if (p != MAP_FAILED) {
             (void)madvise(p, bytes, MADV_HUGEPAGE);  // a hint: ignored where THP is off
-            const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+            const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterMapped);
             if (e == cudaSuccess) {
+                // the device's first writes to the pages, made here rather than
+                // in the first readback into the buffer
+                void* dp = nullptr;
+                if (cudaHostGetDevicePointer(&dp, p, 0) == cudaSuccess && dp) {
+                    launch_touch_pages(dp, bytes, ctx().stream);
+                    HQ_CHECK_CUDA(cudaStreamSynchronize(ctx().stream));
+                } else {
+                    (void)cudaGetLastError();
+                }
                 std::lock_guard<std::mutex> lk(g_host_mu);
                 g_host_mapped[p] = bytes;
                 *out = p;

@@ -165,6 +165,9 @@ void launch_permute_bits(void* state, int n, const int* dest_of, void* stream);
 // bytes from device memory d to a device-mapped pinned host buffer, by `ctas`
 // blocks (a few SMs); stream-ordered
 void launch_readback(const void* d, void* host_mapped, uint64_t bytes, int ctas, void* stream);
+// a zero word in every 4 KB page of a device-mapped host buffer (its first
+// device writes), stream-ordered
+void launch_touch_pages(void* host_mapped, uint64_t bytes, void* stream);
 // the 4-int device error word to a device-mapped host copy, stream-ordered
 void launch_error_readout(const int* d_error, int* h_mapped, void* stream);
 void launch_oshm(const OshmLaunch& p, void* stream);

@@ -391,6 +391,23 @@ __global__ void __launch_bounds__(256) k_permute_tile(float2* __restrict__ a,
     }
 }
 
+// One word per 4 KB page of a freshly registered host buffer, written through
+// its device mapping: the first device writes to each page are slow (on GB300
+// the first 8 GiB readback into a new buffer took about 0.57 s, later ones
+// 45 ms), so they happen when the buffer is made.
+__global__ void k_touch_pages(unsigned int* __restrict__ p, uint64_t words, uint64_t step) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i * step < words; i += stride)
+        p[i * step] = 0u;
+}
+
+void launch_touch_pages(void* host_mapped, uint64_t bytes, void* stream) {
+    const uint64_t words = bytes / 4;
+    if (words == 0) return;
+    k_touch_pages<<<256, 256, 0, (cudaStream_t)stream>>>((unsigned int*)host_mapped, words, 1024);
+    HQ_CHECK_CUDA(cudaGetLastError());
+}
+
 __global__ void k_error_readout(const int* __restrict__ d, int* __restrict__ h) {
     if (threadIdx.x < 4) h[threadIdx.x] = d[threadIdx.x];
 }

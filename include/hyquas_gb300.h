@@ -84,8 +84,11 @@ hq_status hq_set_hbm_budget(uint64_t bytes);
 hq_status hq_hbm_in_use(uint64_t* bytes);
 
 /* Page-locked host buffers for fast state transfers: from 64 MiB up an
- * anonymous mapping with transparent huge pages requested, page-locked with
- * cudaHostRegister; smaller ones (or where that fails) from cudaHostAlloc. */
+ * anonymous mapping with transparent huge pages requested, page-locked and
+ * device-mapped with cudaHostRegister, every page then written once through
+ * the mapping (so the first readback into it runs at full rate; contents are
+ * zero-filled words per 4 KB, otherwise undefined); smaller ones (or where
+ * that fails) from cudaHostAlloc. */
 hq_status hq_host_alloc(uint64_t bytes, void** out);
 /* Frees a buffer from hq_host_alloc. */
 hq_status hq_host_free(void* p);
