@@ -2,7 +2,7 @@
 """Benchmarks on one GB300 (default: the 30-qubit random grid circuit).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload grid30|plain20|qft28|batch|serve]
+                    [--workload grid30|plain20|qft28|batch|serve|remap|dense28|blocked28]
                     [--backend oshm|hybrid|transmm] [--no-cpu-baseline]
 
 grid30 (default, the headline): a step = one full circuit (845 gates:
@@ -19,6 +19,10 @@ ms_per_step is device time per circuit.
                 step Circuit(30) + addGates + compile (program upload = H2D),
                 |0..0> init, run, copy-back of the full state into pinned host
                 memory (D2H) -- the reference's Circuit::run(copy_back=true).
+                Two states alternate so that a circuit's readback (a copy
+                kernel on 8 SMs) runs beside the next circuit; also recorded:
+                the same steps one after another through Circuit.run_to_host,
+                and a new circuit every step (its kernels compiling meanwhile).
   cpu_baseline  the oracle's complex64 OpenMP gate-by-gate port on this host's
                 cores, on a bounded sample (the circuit's first gates), scaled
                 to circuits/s.
@@ -37,6 +41,12 @@ The other workloads print one line each with their own metric:
   serve    Poisson streams at 200, 1000 and 5000 circuits/s (n log-uniform
            12..32, depth 10..60) through the request loop; circuits/s and
            p50/p99 latency against one-at-a-time execution.
+  remap    one in-place pass moving 8 physical bits of a 30-qubit state, and
+           back; GB/s against the measured copy bandwidth.
+  dense28  28 qubits, 10 layers of U3 + CNOT matching: OShareMem-only, hybrid,
+           TransMM-only.
+  blocked28  28 qubits in 7-qubit blocks of deep U3 + CNOT layers joined by
+           single CNOTs, where the hybrid takes TransMM for every group.
 
 Multi-GPU: replicas only (the single-GPU path does not shard); each rank runs
 its own circuit on its own GPU, barrier + max over ranks.
