@@ -37,12 +37,14 @@ double batch_cost(const Partition& part, const std::vector<hq_gate>& gates, int 
 
 }  // namespace
 
-// Tiles per work item: about four items per resident block and level, at most
-// 16 tiles (1 MiB of amplitudes) per item, so that the blocks finish a launch
-// within about one item of each other.
+// Tiles per work item: an eighth of a circuit's tiles, at most 16 (1 MiB of
+// amplitudes).  The items of every circuit of a level interleave, so even the
+// largest circuits need not be split per block; fewer, larger items spend
+// less on the item queue and the dependency counters (512 RY/RZ+CZ circuits:
+// 48,089 items in 133.9 ms against 514,785 one-tile items in 148.7 ms).
 uint32_t batch_chunk_tiles(uint64_t tiles, int slots) {
-    const uint64_t c = tiles / (4 * uint64_t(std::max(1, slots)));
-    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 1), 16);
+    (void)slots;
+    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(tiles / 8, 1), 16);
 }
 
 void batch_release(hq_batch_s* b) {
