@@ -20,7 +20,7 @@ ms_per_step is device time per circuit.
                 |0..0> init, run, copy-back of the full state into pinned host
                 memory (D2H) -- the reference's Circuit::run(copy_back=true).
                 Two states alternate so that a circuit's readback (a copy
-                kernel on 8 SMs) runs beside the next circuit; also recorded:
+                kernel on 4 SMs) runs beside the next circuit; also recorded:
                 the same steps one after another through Circuit.run_to_host,
                 and a new circuit every step (its kernels compiling meanwhile).
   cpu_baseline  the oracle's complex64 OpenMP gate-by-gate port on this host's
@@ -405,7 +405,7 @@ def run_ours(args, dist: Dist):
         fresh_s = dist.max(time.perf_counter() - f0)
         e2e = {"value": dist.ws * args.steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(8 * (1 << n)),
-               "readback": "State.store_async: a copy kernel on 8 SMs writes the pinned buffer "
+               "readback": "State.store_async: a copy kernel on 4 SMs writes the pinned buffer "
                            "while the next step runs on the other SMs; two states alternate",
                "readback_gbs": readback_gbs,
                "pinned_numa_nodes": [b.numa_nodes() for b in pinned],

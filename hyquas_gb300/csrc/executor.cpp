@@ -124,9 +124,11 @@ void state_store_async(hq_state_s* s, void* host) {
     if (mapped && s->bytes >= (size_t(64) << 20) && s->bytes % 16 == 0) {
         // pinned and large: a copy kernel on a few SMs, so that the next
         // circuit's kernels run beside it on the others.  The host link sets
-        // its rate: on GB300 8 blocks of 512 threads write 190 GB/s to pinned
-        // memory, 12 or more 193 GB/s, as the copy engine does.
-        const int ctas = std::min(c.sm_count, 8);
+        // its rate: on GB300 4 blocks of 512 threads write 182 GB/s to pinned
+        // memory, 8 190 GB/s, 12 or more 193 GB/s (the copy engine's rate);
+        // 4 keep 148 SMs for the next circuit and an 8 GiB state still lands
+        // within one 30-qubit circuit's run.
+        const int ctas = std::min(c.sm_count, 4);
         launch_readback(s->d, mapped, s->bytes, ctas, c.copy_stream);
         HQ_CHECK_CUDA(cudaEventRecord(s->copy_done, c.copy_stream));
         if (!c.rb_done) HQ_CHECK_CUDA(cudaEventCreateWithFlags(&c.rb_done, cudaEventDisableTiming));

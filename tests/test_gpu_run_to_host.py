@@ -96,3 +96,36 @@ def test_async_readback_beside_the_next_run(hq):
     sa.wait()
     assert np.array_equal(buf.array, ref_a)
     assert np.array_equal(sb.store(), ref_b)
+
+
+def test_run_to_host_after_a_transmm_group(hq, oracle):
+    """A schedule whose last group is a TransMM group reads back by copy."""
+    n = 21
+    desc = W.blocked_u3_cnot(12, n, 7, 6, 1)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile("transmm")
+    assert all(b == hq.BACKEND_TRANSMM for (b, _, _, _) in c.schedule())
+    buf = hq.PinnedBuffer(1 << n)
+    s = hq.State(n)
+    s.init_zero()
+    c.run_to_host(s, buf.array)
+    cmp = oracle.compare(oracle.run_f64(n, desc), buf.array)
+    assert cmp["max_abs_err"] <= 1e-5 and cmp["one_minus_fidelity"] <= 1e-6, cmp
+
+
+@pytest.mark.parametrize("n,pinned", [(20, True), (20, False), (23, True)])
+def test_async_readback_small_and_unpinned_buffers(hq, n, pinned):
+    """Below 64 MiB, or into pageable memory, store_async copies with the copy
+    engine; from 64 MiB of pinned memory up, with the copy kernel.  All give
+    the bytes of a synchronous store."""
+    c = _compiled(hq, n, W.grid_random(13, 4, n // 4, 4) if n % 4 == 0 else W.grid_random(13, 1, n, 4))
+    ref = _run_and_store(hq, c, n)
+    s = hq.State(n)
+    s.init_zero()
+    c.run_on(s)
+    out = hq.PinnedBuffer(1 << n).array if pinned else np.empty(1 << n, dtype=np.complex64)
+    out[:] = np.complex64(complex(np.nan, np.nan))
+    s.store_async(out)
+    s.wait()
+    assert np.array_equal(out, ref)
