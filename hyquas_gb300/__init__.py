@@ -185,15 +185,25 @@ def device_info():
     return {"sm_count": sm.value, "hbm_bytes": hbm.value, "smem_per_block": smem.value}
 
 
+class _PinnedView:
+    """The numpy view's base: it holds the PinnedBuffer, so the memory stays
+    allocated while any view of it is alive (unless free() is called)."""
+
+    def __init__(self, owner, ptr: int, count: int, dtype):
+        self.owner = owner
+        self.__array_interface__ = {"shape": (int(count),), "typestr": np.dtype(dtype).str,
+                                    "data": (ptr, False), "version": 3}
+
+
 class PinnedBuffer:
-    """Page-locked host memory viewed as a numpy array."""
+    """Page-locked host memory viewed as a numpy array (`array`).  The buffer
+    lives as long as the buffer object or any view of `array`."""
 
     def __init__(self, count: int, dtype=np.complex64):
         self.ptr = C.c_void_p()
         nbytes = int(count) * np.dtype(dtype).itemsize
         check(lib.hq_host_alloc(nbytes, C.byref(self.ptr)))
-        buf = (C.c_char * nbytes).from_address(self.ptr.value)
-        self.array = np.frombuffer(buf, dtype=dtype, count=count)
+        self.array = np.asarray(_PinnedView(self, self.ptr.value, count, dtype))
 
     def numa_nodes(self, samples: int = 16) -> list[int] | None:
         """NUMA node of `samples` pages spread over the buffer (move_pages with

@@ -928,7 +928,9 @@ std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>&
                     // a spill of up to 128 bytes per thread costs less than the 16
                     // warps per SM gain (measured on the 30-qubit grid); beyond that,
                     // one double-buffered CTA of 8 warps per SM
-                    const int need = shape0 == Shape::PAIRED ? 2 : 1;  // RING: bounds ask for more
+                    // PAIRED needs two CTAs per SM; RING one (narrower RING tiles ask
+                    // for more through __launch_bounds__, but one still works)
+                    const int need = shape0 == Shape::PAIRED ? 2 : 1;
                     if (shape0 != Shape::SINGLE && (jk.local_bytes > 128 || jk.blocks_per_sm < need)) {
                         cudaLibraryUnload(jk.lib);
                         int t2 = 0;

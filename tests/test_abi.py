@@ -91,3 +91,28 @@ def test_compile_options_validated_without_device():
     o.backend = 7
     assert hq.lib.hq_plan_groups(10, gates, 1, C.byref(o), C.byref(ng), None, None, None, None,
                                  None, None) == -1
+
+
+def test_pinned_view_keeps_its_buffer_alive():
+    """PinnedBuffer.array's base holds the PinnedBuffer, so a view taken from a
+    temporary buffer object does not outlive the memory (host-only check of
+    the view mechanism, on ordinary memory)."""
+    import gc
+    import weakref
+    import numpy as np
+    import hyquas_gb300 as hq
+
+    class Owner:
+        pass
+
+    backing = np.arange(8, dtype=np.complex64)
+    owner = Owner()
+    ref = weakref.ref(owner)
+    view = np.asarray(hq._PinnedView(owner, backing.ctypes.data, 8, np.complex64))
+    del owner
+    gc.collect()
+    assert ref() is not None
+    assert view.dtype == np.complex64 and view.shape == (8,) and view[3] == backing[3]
+    del view
+    gc.collect()
+    assert ref() is None

@@ -124,7 +124,8 @@ def test_async_readback_small_and_unpinned_buffers(hq, n, pinned):
     s = hq.State(n)
     s.init_zero()
     c.run_on(s)
-    out = hq.PinnedBuffer(1 << n).array if pinned else np.empty(1 << n, dtype=np.complex64)
+    buf = hq.PinnedBuffer(1 << n) if pinned else None
+    out = buf.array if pinned else np.empty(1 << n, dtype=np.complex64)
     out[:] = np.complex64(complex(np.nan, np.nan))
     s.store_async(out)
     s.wait()
