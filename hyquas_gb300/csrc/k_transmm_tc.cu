@@ -495,14 +495,11 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_transmm_tcs(const TransmmLaun
             if ((r >> b) & 1) x |= 1u << p.row_local[b];
         rowslot[r] = tile_swz(x);
     }
-    // physical offset of each column within a tile, for the epilogue's stores
-    uint64_t* coloff = reinterpret_cast<uint64_t*>(smem + SMS_MISC + 2048 - 8 * S::NCOL);
     for (int c = t; c < S::NCOL; c += TS_THREADS) {
         uint32_t x = 0;
         for (int b = 0; b < TC_TILE_BITS - KQ; b++)
             if ((c >> b) & 1) x |= 1u << p.col_local[b];
         colslot[c] = tile_swz(x);
-        coloff[c] = local_to_phys(x, TC_TILE_BITS, p.tile_phys);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -627,23 +624,15 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_transmm_tcs(const TransmmLaun
             cp_async_commit();
         };
         float2* R = reinterpret_cast<float2*>(smem + SMS_R);
-        // results of tile j: TMEM buffer j&1 straight to HBM (R already holds
-        // the next tile).  Warp (q, h): TMEM lanes 32 q .. 32 q + 31 of half
-        // m = h (KQ = 8) or of columns 32 h .. (KQ = 7); a thread keeps one row.
-        const int eq = warp & 3, eh = warp >> 2;
-        const int em = S::MB == 2 ? eh : 0, ec0 = S::MB == 2 ? 0 : 32 * eh;
-        const int erow = 128 * em + 32 * eq + lane;  // row of the group
-        uint64_t rowoff = 0;
-        {
-            uint32_t x = 0;
-            for (int bb = 0; bb < KQ; bb++)
-                if ((erow >> bb) & 1) x |= 1u << p.row_local[bb];
-            rowoff = local_to_phys(x, TC_TILE_BITS, p.tile_phys);
-        }
+        // results of tile j: TMEM buffer j&1 -> R -> HBM.  Warp (q, h): TMEM
+        // lanes 32 q .. 32 q + 31 of half m = h (KQ = 8) or of columns 32 h .. (KQ = 7)
         auto epilogue = [&](uint64_t j) {
             const uint32_t b = uint32_t(j & 1);
-            const uint32_t col = tmem + ((uint32_t)(32 * eq) << 16) + 256 * b + 3 * S::NCOL * em + ec0;
-            float2* __restrict__ g = state + tbase(j) + rowoff;
+            const int q = warp & 3, h = warp >> 2;
+            const int m = S::MB == 2 ? h : 0, c0 = S::MB == 2 ? 0 : 32 * h;
+            const int i = 128 * m + 32 * q + lane;  // row of the group
+            const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + 256 * b + 3 * S::NCOL * m + c0;
+            const uint32_t rs = rowslot[i];
 #pragma unroll
             for (int c8 = 0; c8 < 4; c8++) {
                 uint32_t vp[8], vq[8], vi[8];
@@ -652,10 +641,17 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_transmm_tcs(const TransmmLaun
                 tmem_ld8(col + 2 * S::NCOL + 8 * c8, vi);
 #pragma unroll
                 for (int c = 0; c < 8; c++)
-                    g[coloff[ec0 + 8 * c8 + c]] =
+                    R[rs ^ colslot[c0 + 8 * c8 + c]] =
                         make_float2(__uint_as_float(vp[c]) - __uint_as_float(vq[c]), __uint_as_float(vi[c]));
             }
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            workers_sync();
+            float2* gdst = state + tbase(j) + toff;
+            const float4* R4 = reinterpret_cast<const float4*>(R);
+#pragma unroll
+            for (int mm = 0; mm < 16; mm++)
+                *reinterpret_cast<float4*>(gdst + poff[mm]) = R4[(tsl ^ pslot[mm]) >> 1];
+            workers_sync();
         };
         bool failed = false;
         load(0);
@@ -719,9 +715,9 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_transmm_tcs(const TransmmLaun
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(m_bfull) : "memory");
-            workers_sync();  // R is read: the next tile's copies may land in it
-            load(j + 1);
+            workers_sync();  // R is read: the epilogue may write over it
             if (j > 0) epilogue(j - 1);
+            load(j + 1);
         }
         if (!failed && J > 0) {
             const bool ok = mbar_wait(m_acc + 8 * uint32_t((J - 1) & 1), uint32_t(((J - 1) >> 1) & 1));
