@@ -131,7 +131,10 @@ hq_status hq_state_store(hq_state s, float* host_amps);
  * the work already queued on s, so a circuit on another state overlaps it.
  * host_amps must stay valid (and should be pinned, hq_host_alloc) until
  * hq_state_wait(s); later work that writes s waits for the copy on the device.
- * hq_state_store's asynchronous form, for pipelined readback. */
+ * Into pinned memory of 64 MiB or more the copy is a kernel on 4 SMs, and the
+ * library's group kernels launch on the other SMs while it is in flight;
+ * otherwise copy-engine transfers.  hq_state_store's asynchronous form, for
+ * pipelined readback. */
 hq_status hq_state_store_async(hq_state s, float* host_amps);
 /* Block until s's pending asynchronous copy has landed in host memory. */
 hq_status hq_state_wait(hq_state s);
