@@ -69,3 +69,20 @@ def test_tile_width_is_chosen_per_circuit():
         assert {x["width"] for x in fixed} == {t} and len(fixed) > len(auto)
     small = hq.plan_groups(9, W.to_gates(W.grid_random(3, 3, 3, 6)))
     assert {x["width"] for x in small} == {9}
+
+
+def test_hybrid_keeps_the_best_whole_schedule():
+    """The hybrid's per-group choice is set against the OShareMem-only and
+    TransMM-only schedules and the predicted-fastest kept: deep dense 7-qubit
+    blocks fuse into TransMM groups throughout, the grid circuit stays
+    OShareMem."""
+    import hyquas_gb300 as hq
+    from hyquas_gb300 import workloads as W
+
+    def kinds(n, g, backend):
+        return [x["backend"] for x in hq.plan_groups(n, g, backend=backend)]
+
+    blocked = W.to_gates(W.blocked_u3_cnot(11, 28, 7, 10, 2))
+    assert set(kinds(28, blocked, hq.BACKEND_HYBRID)) == {hq.BACKEND_TRANSMM}
+    grid = W.to_gates(W.grid_random(2, 5, 6, 20))
+    assert set(kinds(30, grid, hq.BACKEND_HYBRID)) == {hq.BACKEND_OSHM}
