@@ -521,6 +521,13 @@ double snap(double x) {
 
 // the shear form of a rotation by phi: phi reduced to [-pi/2, pi/2] (a rotation
 // by pi is a negation), a = -tan(phi/2), b = sin(phi)
+// a real 2x2 [[c, -s], [s, c]] with c^2 + s^2 = 1 (RY and its powers)
+bool is_rotation(const hq_gate& g) {
+    const double c = g.mat[0], s = g.mat[4];
+    return std::fabs(g.mat[6] - c) < 1e-12 && std::fabs(g.mat[2] + s) < 1e-12 &&
+           std::fabs(c * c + s * s - 1.0) < 1e-12;
+}
+
 void shear(double phi, OshmOp& o) {
     const double pi = std::acos(-1.0);
     if (phi > pi / 2) {
@@ -713,6 +720,9 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
                     o.kind = (uint8_t)had;  // runs without its 1/sqrt2: deferred
                     pending_scale *= rsqrt2;
                     pending_count++;
+                } else if (rt >= 1 && o.creg == 0 && real && is_rotation(g)) {
+                    o.kind = OP_RROT;  // three shears per plane instead of a 2x2 product
+                    shear(std::atan2(g.mat[4], g.mat[0]), o);
                 } else if (rt >= 1 && o.creg == 0 && real) {
                     o.kind = OP_REAL;
                 } else if (rt >= 1 && o.creg == 0 && imoff) {
@@ -850,12 +860,14 @@ double cost_oshm(int n, int nphases, const std::vector<hq_gate>& gates, int k) {
 
 // Arithmetic of a non-diagonal gate in the register phases, in units of one
 // packed add per amplitude (the sqrt(X) / sqrt(Y) / H gates): an exchange is
-// register renaming, a real or imaginary-off-diagonal rotation one multiply
-// and one fused multiply-add per component, a general complex 2x2 four.
+// register renaming, a real rotation three shears per plane, another real or
+// imaginary-off-diagonal 2x2 one multiply and one fused multiply-add per
+// component, a general complex 2x2 four.
 double oshm_gate_units(const hq_gate& g) {
     if (is_x_like(g)) return 0.25;
     if (hadamard_like(g) >= 0) return 1.0;
     const bool real = g.mat[1] == 0 && g.mat[3] == 0 && g.mat[5] == 0 && g.mat[7] == 0;
+    if (real && is_rotation(g)) return 1.5;
     const bool imoff = g.mat[1] == 0 && g.mat[7] == 0 && g.mat[2] == 0 && g.mat[4] == 0;
     return (real || imoff) ? 2.0 : 4.0;
 }

@@ -38,16 +38,19 @@ enum OshmOpKind : uint8_t {
     OP_DREG = 7,   // diag(d0, d1) on a register qubit (d0 = m0 m1, d1 = m6 m7)
     OP_NEGHI = 8,  // diag(1, -1) on a register qubit (Z, CZ)
     OP_DOUT = 9,   // diag(d0, d1) whose target is outside the register set
-    OP_DROT = 11   // diag(1, e^{i phi}) on a register qubit: the high amplitude's
+    OP_DROT = 11,  // diag(1, e^{i phi}) on a register qubit: the high amplitude's
                    // (re, im) rotated by phi in place with three shears
                    // x += a y; y += b x; x += a y (a = -tan(phi/2) = m0, b = sin(phi) = m1),
                    // then negated when OPF_NEG (phi was reduced by pi)
+    OP_RROT = 12   // [[c, -s], [s, c]] (RY and the like) on a register qubit J >= 1:
+                   // (lo, hi) rotated by phi = atan2(s, c) with the same three shears
+                   // in the real and in the imaginary plane (m0, m1, OPF_NEG as DROT)
 };
 enum OshmOpFlags : uint8_t {
     OPF_D0_ONE = 1,   // diagonal op: d0 == 1
     OPF_COUT = 2,     // has controls outside the register set (`cout`)
     OPF_CREG = 4,     // has controls on register qubits (`creg`)
-    OPF_NEG = 8       // OP_DROT: negate the result
+    OPF_NEG = 8       // OP_DROT, OP_RROT: negate the result
 };
 
 struct alignas(16) OshmOp {

@@ -227,7 +227,7 @@ struct Gen {
                (full && (kind == OP_SY || kind == OP_SX));
     }
     static bool pair_needs_align(int kind, bool full, bool has_cout) {
-        if (kind == OP_U || kind == OP_REAL || kind == OP_IMOFF) return true;
+        if (kind == OP_U || kind == OP_REAL || kind == OP_IMOFF || kind == OP_RROT) return true;
         if (kind == OP_H || kind == OP_SY || kind == OP_SX || kind == OP_X)
             return !pair_fast(kind, full, has_cout);
         return false;
@@ -365,7 +365,8 @@ struct Gen {
                 consts(nm, v, 6);
                 break;
             }
-            case OP_DROT: {
+            case OP_DROT:
+            case OP_RROT: {
                 const char* nm[] = {"sa", "sb"};
                 const float v[] = {m[0], m[1]};
                 consts(nm, v, 2);
@@ -493,6 +494,23 @@ struct Gen {
                 case OP_DROT:
                     shear(R(h), I(h), "hr", "hi");
                     break;
+                case OP_RROT: {
+                    // (lo, hi) rotated in the real and in the imaginary plane;
+                    // a negation (phi reduced by pi) flips both slots' signs,
+                    // at run time only under a run-time control
+                    const bool xneg = negf_op && has_cout;
+                    for (int comp = 0; comp < 2; comp++) {
+                        o << "{ v2 x = " << (comp ? "li" : "lr") << ", y = " << (comp ? "hi" : "hr")
+                          << "; x = vfma(sa, y, x); y = vfma(sb, x, y); x = vfma(sa, y, x); ";
+                        if (xneg) o << "x ^= 0x8000000080000000ull; y ^= 0x8000000080000000ull; ";
+                        o << (comp ? I(j) : R(j)) << " = x; " << (comp ? I(h) : R(h)) << " = y; }\n";
+                    }
+                    if (negf_op && !has_cout) {
+                        sn[j] = !sn[j];
+                        sn[h] = !sn[h];
+                    }
+                    break;
+                }
                 case OP_NEGHI: {
                     // sign flips as bit XORs: they run on the ALU pipe, not the FMA pipe
                     const char* mask = k0 && k1 ? "0x8000000080000000ull"
