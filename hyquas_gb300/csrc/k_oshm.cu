@@ -246,19 +246,14 @@ __device__ __forceinline__ void op_drot(Amps<NV>& A, const float (&m)[8], bool n
 }
 
 // [[c, -s], [s, c]]: (lo, hi) rotated in the real and in the imaginary plane
-// with three shears each, negated when the angle was reduced by pi
+// with three shears each (the negation of an angle reduced by pi covers every
+// register of the thread, so apply_op folds it into the phase factor)
 template <int J, int NV>
-__device__ __forceinline__ void op_rrot(Amps<NV>& A, const float (&m)[8], bool neg) {
-    const v2 a = vdup(m[0]), b = vdup(m[1]), sgn = 0x8000000080000000ull;
+__device__ __forceinline__ void op_rrot(Amps<NV>& A, const float (&m)[8]) {
+    const v2 a = vdup(m[0]), b = vdup(m[1]);
     HQ_PAIRS_IP(J, NV, {
         ip_shear(A.re[j], A.re[h], a, b);
         ip_shear(A.im[j], A.im[h], a, b);
-        if (neg) {
-            ip_xor(A.re[j], sgn);
-            ip_xor(A.re[h], sgn);
-            ip_xor(A.im[j], sgn);
-            ip_xor(A.im[h], sgn);
-        }
     })
 }
 
@@ -476,6 +471,7 @@ __device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hd
         }
         return;
     }
+    if (kind == OP_RROT && (flags & OPF_NEG)) acc = make_float2(-acc.x, -acc.y);
     switch (HQ_CODE(flags & OPF_CREG, kind, tb)) {
         HQ_CASE_LANE(OP_X, (lane_x<NV>(A, creg)))
         HQ_CASE_LANE(OP_DREG, (lane_diag<NV>(A, m, creg)))
@@ -493,7 +489,7 @@ __device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hd
         HQ_CASE_J(0, OP_DREG, (op_dreg<J, NV>(A, m, d0one)))
         HQ_CASE_J(0, OP_NEGHI, (op_neghi<J, NV>(A)))
         HQ_CASE_J(0, OP_DROT, (op_drot<J, NV>(A, m, (flags & OPF_NEG) != 0)))
-        HQ_CASE_J(0, OP_RROT, (op_rrot<J, NV>(A, m, (flags & OPF_NEG) != 0)))
+        HQ_CASE_J(0, OP_RROT, (op_rrot<J, NV>(A, m)))
         HQ_CASE_J(1, OP_X, (ctl_x<J, NV>(A, creg)))
         HQ_CASE_J(1, OP_NEGHI, (ctl_neghi<J, NV>(A, creg)))
         HQ_CASE_J(1, OP_DREG, (ctl_diag<J, NV>(A, m, creg, d0one)))
