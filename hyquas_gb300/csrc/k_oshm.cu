@@ -361,47 +361,6 @@ __device__ __forceinline__ void ctl_diag(Amps<NV>& A, const float (&m)[8], uint3
     })
 }
 
-// Sign flips as XORs of the sign bits (ALU pipe, no constants to build).
-// sel_neg: every register whose index has the creg bits set;
-// ctl_neghi: the high half (register bit J set) of those pairs.
-template <int NV>
-__device__ __forceinline__ void sel_neg(Amps<NV>& A, uint32_t creg) {
-#pragma unroll
-    for (int j = 0; j < NV; j++) {
-        const bool o0 = (uint32_t(2 * j) & creg) == creg;
-        const bool o1 = (uint32_t(2 * j + 1) & creg) == creg;
-        if (!o0 && !o1) continue;
-        const v2 msk = (o0 ? 0x80000000ull : 0ull) | (o1 ? 0x8000000000000000ull : 0ull);
-        ip_xor(A.re[j], msk);
-        ip_xor(A.im[j], msk);
-    }
-}
-
-// target = the vector lane: the odd amplitude of each selected vector
-template <int NV>
-__device__ __forceinline__ void lane_neghi(Amps<NV>& A, uint32_t creg) {
-    const v2 msk = 0x8000000000000000ull;
-#pragma unroll
-    for (int j = 0; j < NV; j++) {
-        if ((uint32_t(2 * j) & creg) != creg) continue;
-        ip_xor(A.re[j], msk);
-        ip_xor(A.im[j], msk);
-    }
-}
-
-template <int J, int NV>
-__device__ __forceinline__ void ctl_neghi(Amps<NV>& A, uint32_t creg) {
-    HQ_PAIRS_IP(J, NV, {
-        const bool o0 = (uint32_t(2 * j) & creg) == creg;
-        const bool o1 = (uint32_t(2 * j + 1) & creg) == creg;
-        if (o0 || o1) {
-            const v2 msk = (o0 ? 0x80000000ull : 0ull) | (o1 ? 0x8000000000000000ull : 0ull);
-            ip_xor(A.re[h], msk);
-            ip_xor(A.im[h], msk);
-        }
-    })
-}
-
 // multiply the registers selected by creg by the complex factor f
 template <int NV>
 __device__ __forceinline__ void scale_sel(Amps<NV>& A, float2 f, uint32_t creg) {
@@ -463,19 +422,14 @@ __device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hd
         if (creg == 0)
             acc = cmul(acc, f);
         else
-        {
-            if (f.x == -1.f && f.y == 0.f)
-                sel_neg<NV>(A, creg);
-            else
-                scale_sel<NV>(A, f, creg);
-        }
+            scale_sel<NV>(A, f, creg);
         return;
     }
     if (kind == OP_RROT && (flags & OPF_NEG)) acc = make_float2(-acc.x, -acc.y);
     switch (HQ_CODE(flags & OPF_CREG, kind, tb)) {
         HQ_CASE_LANE(OP_X, (lane_x<NV>(A, creg)))
         HQ_CASE_LANE(OP_DREG, (lane_diag<NV>(A, m, creg)))
-        HQ_CASE_LANE(OP_NEGHI, (lane_neghi<NV>(A, creg)))
+        HQ_CASE_LANE(OP_NEGHI, (lane_diag<NV>(A, m, creg)))
         HQ_CASE_LANE(OP_U, (lane_u<NV>(A, m, creg)))
         HQ_CASE_LANE(OP_REAL, (lane_u<NV>(A, m, creg)))
         HQ_CASE_LANE(OP_IMOFF, (lane_u<NV>(A, m, creg)))
@@ -491,7 +445,7 @@ __device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hd
         HQ_CASE_J(0, OP_DROT, (op_drot<J, NV>(A, m, (flags & OPF_NEG) != 0)))
         HQ_CASE_J(0, OP_RROT, (op_rrot<J, NV>(A, m)))
         HQ_CASE_J(1, OP_X, (ctl_x<J, NV>(A, creg)))
-        HQ_CASE_J(1, OP_NEGHI, (ctl_neghi<J, NV>(A, creg)))
+        HQ_CASE_J(1, OP_NEGHI, (ctl_diag<J, NV>(A, m, creg, true)))
         HQ_CASE_J(1, OP_DREG, (ctl_diag<J, NV>(A, m, creg, d0one)))
         HQ_CASE_J(1, OP_U, (ctl_u<J, NV>(A, m, creg)))
         HQ_CASE_J(1, OP_REAL, (ctl_u<J, NV>(A, m, creg)))
