@@ -3,7 +3,6 @@
 // g++-compiled host code can include it.
 #pragma once
 
-#include <cstddef>
 #include <cstdint>
 
 #include "../../include/hyquas_gb300.h"
@@ -66,10 +65,6 @@ struct alignas(16) OshmOp {
     float m[8];
 };
 static_assert(sizeof(OshmOp) == 64, "OshmOp layout");
-// the interpreter reads an op as four 16-byte words: header, target mask, matrix halves
-static_assert(offsetof(OshmOp, creg) == 4 && offsetof(OshmOp, cout) == 8 && offsetof(OshmOp, tout) == 16 &&
-                  offsetof(OshmOp, m) == 32,
-              "OshmOp word layout");
 
 constexpr int OSHM_MAX_R = 5;      // register bits per thread (32 amplitudes)
 constexpr int OSHM_MAX_K = 13;     // tile bits

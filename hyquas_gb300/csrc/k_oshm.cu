@@ -392,10 +392,8 @@ __device__ __forceinline__ void scale_sel(Amps<NV>& A, float2 f, uint32_t creg) 
     case HQ_CODE(1, KIND, 0): CALL; break;
 
 template <int R>
-// The op arrives whole in registers (its 64 bytes as four uint4: header,
-// target mask, matrix halves), loaded while the previous op ran.
-__device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hdr, const uint4 ht,
-                                         const uint4 m0v, const uint4 m1v, uint64_t pidx,
+__device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hdr,
+                                         const OshmOp* __restrict__ op, uint64_t pidx,
                                          float2& acc) {
     constexpr int NV = 1 << (R - 1);
     const uint32_t kind = hdr.x & 0xffu, tb = (hdr.x >> 8) & 0xffu, flags = (hdr.x >> 16) & 0xffu;
@@ -406,10 +404,10 @@ __device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hd
     }
     float m[8];
     if (kind != OP_H && kind != OP_SY && kind != OP_SX && kind != OP_X && kind != OP_NEGHI) {
-        m[0] = __uint_as_float(m0v.x); m[1] = __uint_as_float(m0v.y);
-        m[2] = __uint_as_float(m0v.z); m[3] = __uint_as_float(m0v.w);
-        m[4] = __uint_as_float(m1v.x); m[5] = __uint_as_float(m1v.y);
-        m[6] = __uint_as_float(m1v.z); m[7] = __uint_as_float(m1v.w);
+        const float4* mp = reinterpret_cast<const float4*>(op->m);
+        const float4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
+        m[0] = m0.x; m[1] = m0.y; m[2] = m0.z; m[3] = m0.w;
+        m[4] = m1.x; m[5] = m1.y; m[6] = m1.z; m[7] = m1.w;
     } else {
         // the sign flip as a diagonal with d0 = 1, d1 = -1
         m[0] = 1.f; m[1] = 0.f; m[2] = 0.f; m[3] = 0.f;
@@ -417,7 +415,7 @@ __device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hd
     }
     const bool d0one = (flags & OPF_D0_ONE) != 0;
     if (kind == OP_DOUT) {
-        const uint64_t tout = (uint64_t(ht.y) << 32) | ht.x;
+        const uint64_t tout = __ldg(reinterpret_cast<const unsigned long long*>(&op->tout));
         const bool hiset = (pidx & tout) != 0;
         if (!hiset && d0one) return;
         const float2 f = hiset ? make_float2(m[6], m[7]) : make_float2(m[0], m[1]);
@@ -503,19 +501,13 @@ __device__ __forceinline__ void run_phases(const OshmLaunch& p, float4* buf, uin
             }
 
             float2 acc = make_float2(1.f, 0.f);
-            const uint4* __restrict__ opw = reinterpret_cast<const uint4*>(p.ops);  // 4 per op
-            uint4 n0 = make_uint4(0, 0, 0, 0), n1 = n0, n2 = n0, n3 = n0;
-            if (P.op_begin < P.op_end) {
-                const uint4* q = opw + 4 * size_t(P.op_begin);
-                n0 = __ldg(q); n1 = __ldg(q + 1); n2 = __ldg(q + 2); n3 = __ldg(q + 3);
-            }
+            const OshmOp* __restrict__ ops = p.ops;
+            uint4 nxt = make_uint4(0, 0, 0, 0);
+            if (P.op_begin < P.op_end) nxt = __ldg(reinterpret_cast<const uint4*>(ops + P.op_begin));
             for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) {
-                const uint4 c0 = n0, c1 = n1, c2 = n2, c3 = n3;
-                if (oi + 1 < P.op_end) {
-                    const uint4* q = opw + 4 * size_t(oi + 1);
-                    n0 = __ldg(q); n1 = __ldg(q + 1); n2 = __ldg(q + 2); n3 = __ldg(q + 3);
-                }
-                apply_op<R>(A, c0, c1, c2, c3, pidx, acc);
+                const uint4 hdr = nxt;
+                if (oi + 1 < P.op_end) nxt = __ldg(reinterpret_cast<const uint4*>(ops + oi + 1));
+                apply_op<R>(A, hdr, ops + oi, pidx, acc);
             }
             float2 f = acc;
             if (P.scale != 1.f) f = make_float2(f.x * P.scale, f.y * P.scale);
