@@ -624,12 +624,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_transmm_tcs(const TransmmLaun
             cp_async_commit();
         };
         float2* R = reinterpret_cast<float2*>(smem + SMS_R);
-        // The results of tile j are staged in the B buffer (free once tile j's
-        // MMAs have completed and before tile j + 1's B is built; it is the
-        // size of a tile), so R only ever holds raw tiles and the next tile's
-        // copies go out as soon as its B is built.
-        float2* E = reinterpret_cast<float2*>(smem + SMS_B);
-        // results of tile j: TMEM buffer j&1 -> E -> HBM.  Warp (q, h): TMEM
+        // results of tile j: TMEM buffer j&1 -> R -> HBM.  Warp (q, h): TMEM
         // lanes 32 q .. 32 q + 31 of half m = h (KQ = 8) or of columns 32 h .. (KQ = 7)
         auto epilogue = [&](uint64_t j) {
             const uint32_t b = uint32_t(j & 1);
@@ -646,17 +641,17 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_transmm_tcs(const TransmmLaun
                 tmem_ld8(col + 2 * S::NCOL + 8 * c8, vi);
 #pragma unroll
                 for (int c = 0; c < 8; c++)
-                    E[rs ^ colslot[c0 + 8 * c8 + c]] =
+                    R[rs ^ colslot[c0 + 8 * c8 + c]] =
                         make_float2(__uint_as_float(vp[c]) - __uint_as_float(vq[c]), __uint_as_float(vi[c]));
             }
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             workers_sync();
             float2* gdst = state + tbase(j) + toff;
-            const float4* E4 = reinterpret_cast<const float4*>(E);
+            const float4* R4 = reinterpret_cast<const float4*>(R);
 #pragma unroll
             for (int mm = 0; mm < 16; mm++)
-                *reinterpret_cast<float4*>(gdst + poff[mm]) = E4[(tsl ^ pslot[mm]) >> 1];
-            workers_sync();  // E is read: the next B may be built over it
+                *reinterpret_cast<float4*>(gdst + poff[mm]) = R4[(tsl ^ pslot[mm]) >> 1];
+            workers_sync();
         };
         bool failed = false;
         load(0);
@@ -671,7 +666,6 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_transmm_tcs(const TransmmLaun
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                epilogue(j - 1);
             }
             {
                 unsigned char* B = smem + SMS_B;
@@ -721,7 +715,8 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_transmm_tcs(const TransmmLaun
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(m_bfull) : "memory");
-            workers_sync();  // R is read: the next tile's copies may land in it
+            workers_sync();  // R is read: the epilogue may write over it
+            if (j > 0) epilogue(j - 1);
             load(j + 1);
         }
         if (!failed && J > 0) {
