@@ -9,6 +9,7 @@
 // Persistent blocks take items in queue order; an item of group g waits
 // (bounded) until every tile of groups < g of its circuit is written.
 #include <algorithm>
+#include <queue>
 #include <cstring>
 
 #include "batch.h"
@@ -127,34 +128,85 @@ void batch_compile(hq_batch_s* b, const hq_compile_options* opt) {
         }
         ops.insert(ops.end(), progs[i].ops.begin(), progs[i].ops.end());
     }
+    // Item order: a list schedule of the launch simulated on the host.  The
+    // device hands items out in queue order, and an item whose circuit's
+    // previous group is not finished makes its block wait; so the queue is the
+    // order in which `slots` workers would start the items if each item ran
+    // for its estimated time (tiles x the group's ops and phases), an item
+    // becoming ready when every item of its circuit's previous group has
+    // finished, and a free worker taking the ready item of the circuit with
+    // the most estimated work left (its critical path).  An item is queued
+    // only after all its predecessors (they finished first in the
+    // simulation), so the bounded waits always end.
     std::vector<BatchItem> items;
-    uint32_t levels = 0;
-    for (const BatchEntry& e : b->entries) levels = std::max(levels, e.ngroups);
-    std::vector<uint32_t> order(b->entries.size());
-    for (uint32_t i = 0; i < order.size(); i++) order[i] = i;
-    // deepest circuits first inside a level, so their chains start early
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
-        const BatchEntry &a = b->entries[x], &c = b->entries[y];
-        if (a.ngroups != c.ngroups) return a.ngroups > c.ngroups;
-        return a.n > c.n;
-    });
-    for (uint32_t g = 0; g < levels; g++) {
-        for (uint32_t ci : order) {
+    {
+        struct Level {
+            uint32_t circuit, group;
+            uint64_t tiles;
+            uint32_t chunk;
+            double item_t;  // estimated time of one item (arbitrary units)
+        };
+        std::vector<std::vector<Level>> lv(b->entries.size());
+        std::vector<double> left(b->entries.size(), 0.0);
+        for (uint32_t ci = 0; ci < b->entries.size(); ci++) {
             const BatchEntry& e = b->entries[ci];
-            if (g >= e.ngroups) continue;
-            const uint64_t tiles = uint64_t(1) << (e.n - e.k);
+            const uint64_t tiles = e.ngroups ? uint64_t(1) << (e.n - e.k) : 0;
             HQ_REQUIRE(tiles * e.ngroups < (uint64_t(1) << 32), HQ_ERR_UNSUPPORTED,
                        "batch: circuit %u has too many tiles for the 32-bit item counters", ci);
-            const uint32_t ch = batch_chunk_tiles(tiles, slots);
-            for (uint64_t u = 0; u < tiles; u += ch) {
+            for (uint32_t g = 0; g < e.ngroups; g++) {
+                const OshmProgram& pr = progs[e.group0 + g];
+                const uint32_t ch = batch_chunk_tiles(tiles, slots);
+                const double per_tile = 8.0 + double(pr.ops.size()) + 4.0 * double(pr.phases.size());
+                lv[ci].push_back({ci, g, tiles, ch, per_tile * double(ch) * double(1u << e.k) / 8192.0});
+                left[ci] += per_tile * double(tiles) * double(1u << e.k) / 8192.0 / double(slots);
+            }
+        }
+        // ready queue: (priority = estimated work left, circuit, next item of its level)
+        using Ready = std::pair<double, uint32_t>;
+        std::priority_queue<Ready> ready;
+        std::vector<uint32_t> level_of(b->entries.size(), 0);
+        std::vector<uint64_t> next_tile(b->entries.size(), 0), done_items(b->entries.size(), 0);
+        for (uint32_t ci = 0; ci < b->entries.size(); ci++)
+            if (!lv[ci].empty()) ready.push({left[ci], ci});
+        // workers: (time free, worker); running items finish events
+        using Fin = std::pair<double, uint32_t>;  // (finish time, circuit)
+        std::priority_queue<Fin, std::vector<Fin>, std::greater<Fin>> running;
+        double now = 0.0;
+        int busy = 0;
+        auto level_items = [&](uint32_t ci) {
+            const Level& L = lv[ci][level_of[ci]];
+            return (L.tiles + L.chunk - 1) / L.chunk;
+        };
+        while (!ready.empty() || !running.empty()) {
+            while (busy < slots && !ready.empty()) {
+                const uint32_t ci = ready.top().second;
+                ready.pop();
+                const Level& L = lv[ci][level_of[ci]];
+                const uint64_t u = next_tile[ci];
                 BatchItem it;
-                it.group = e.group0 + g;
+                it.group = b->entries[ci].group0 + L.group;
                 it.circuit = ci;
                 it.tile0 = (uint32_t)u;
-                it.count = (uint32_t)std::min<uint64_t>(ch, tiles - u);
-                it.need = (uint32_t)(g * tiles);
-                it.flags = g == 0 ? ITEM_FIRST : 0;
+                it.count = (uint32_t)std::min<uint64_t>(L.chunk, L.tiles - u);
+                it.need = (uint32_t)(L.group * L.tiles);
+                it.flags = L.group == 0 ? ITEM_FIRST : 0;
                 items.push_back(it);
+                next_tile[ci] = u + it.count;
+                running.push({now + L.item_t, ci});
+                busy++;
+                if (next_tile[ci] < L.tiles) ready.push({left[ci], ci});  // more of this level
+            }
+            if (running.empty()) break;
+            const Fin f = running.top();
+            running.pop();
+            now = f.first;
+            busy--;
+            const uint32_t ci = f.second;
+            left[ci] = std::max(0.0, left[ci] - lv[ci][level_of[ci]].item_t / double(slots));
+            if (++done_items[ci] == level_items(ci)) {  // the level is complete: the next one is ready
+                done_items[ci] = 0;
+                next_tile[ci] = 0;
+                if (++level_of[ci] < lv[ci].size()) ready.push({left[ci], ci});
             }
         }
     }
