@@ -716,16 +716,16 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
                 const int had = hadamard_like(g);
                 if (is_x_like(g)) {
                     o.kind = OP_X;
-                } else if (rt >= 1 && o.creg == 0 && o.cout == 0 && had >= 0) {
+                } else if (o.creg == 0 && o.cout == 0 && had >= 0) {
                     o.kind = (uint8_t)had;  // runs without its 1/sqrt2: deferred
                     pending_scale *= rsqrt2;
                     pending_count++;
                 } else if (rt >= 1 && o.creg == 0 && real && is_rotation(g)) {
                     o.kind = OP_RROT;  // three shears per plane instead of a 2x2 product
                     shear(std::atan2(g.mat[4], g.mat[0]), o);
-                } else if (rt >= 1 && o.creg == 0 && real) {
+                } else if (o.creg == 0 && real) {
                     o.kind = OP_REAL;
-                } else if (rt >= 1 && o.creg == 0 && imoff) {
+                } else if (o.creg == 0 && imoff) {
                     o.kind = OP_IMOFF;
                 } else {
                     o.kind = OP_U;

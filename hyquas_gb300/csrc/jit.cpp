@@ -317,6 +317,44 @@ struct Gen {
                     o << "{ const v2 a = " << R(j) << ", b = " << I(j) << "; " << R(j)
                       << " = vfma(In, b, vmul(Rr, a)); " << I(j) << " = vfma(Ii, a, vmul(Rr, b)); }\n";
                 }
+            } else if (kind == OP_REAL || kind == OP_IMOFF || kind == OP_H || kind == OP_SY ||
+                       kind == OP_SX) {
+                // the other lane from a swapped copy, both lanes' coefficients in
+                // one packed constant: one or two instructions per component (the
+                // two lanes of a vector always share their scale)
+                if (kind == OP_REAL)
+                    o << "const v2 P = vpack(" << flit(m[0]) << ", " << flit(m[6]) << "), S = vpack("
+                      << flit(m[2]) << ", " << flit(m[4]) << ");\n";
+                else if (kind == OP_IMOFF)
+                    o << "const v2 P = vpack(" << flit(m[0]) << ", " << flit(m[6]) << "), X = vpack("
+                      << flit(m[3]) << ", " << flit(m[5]) << "), Xn = vpack(" << flit(-m[3]) << ", "
+                      << flit(-m[5]) << ");\n";
+                else if (kind == OP_H)
+                    o << "const v2 K = vpack(1.f, -1.f);\n";
+                else if (kind == OP_SY)
+                    o << "const v2 K = vpack(-1.f, 1.f);\n";
+                for (int j = 0; j < nv; j++) {
+                    if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
+                    o << "{ const v2 a = " << R(j) << ", b = " << I(j) << ", as = vswap(a), bs = vswap(b); ";
+                    switch (kind) {
+                        case OP_REAL:  // (a lo + b hi, c lo + d hi)
+                            o << R(j) << " = vfma(S, as, vmul(P, a)); " << I(j) << " = vfma(S, bs, vmul(P, b));";
+                            break;
+                        case OP_IMOFF:  // (a lo + i b hi, i c lo + d hi)
+                            o << R(j) << " = vfma(Xn, bs, vmul(P, a)); " << I(j) << " = vfma(X, as, vmul(P, b));";
+                            break;
+                        case OP_H:  // (lo + hi, lo - hi)
+                            o << R(j) << " = vfma(K, a, as); " << I(j) << " = vfma(K, b, bs);";
+                            break;
+                        case OP_SY:  // (lo - hi, lo + hi)
+                            o << R(j) << " = vfma(K, as, a); " << I(j) << " = vfma(K, bs, b);";
+                            break;
+                        default:  // sqrt(X): (lo - i hi, hi - i lo)
+                            o << R(j) << " = vadd(a, bs); " << I(j) << " = vsub(b, as);";
+                            break;
+                    }
+                    o << " }\n";
+                }
             } else {
                 o << "const v2 P = vpack(" << flit(m[0]) << ", " << flit(m[6]) << "), Q = vpack("
                   << flit(m[1]) << ", " << flit(m[7]) << "), Qn = vpack(" << flit(-m[1]) << ", "

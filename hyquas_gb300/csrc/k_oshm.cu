@@ -302,6 +302,89 @@ __device__ __forceinline__ void lane_diag(Amps<NV>& A, const float (&m)[8], uint
     }
 }
 
+// Lane ops with a structured matrix: the other lane's value comes from a
+// swapped copy (register renaming) and one packed constant holds both lanes'
+// coefficients, so a component costs one or two packed instructions instead
+// of four.  In place, like the helpers above.
+// x <- P x + S swap(x): real [[a, b], [c, d]] with P = (a, d), S = (b, c)
+__device__ __forceinline__ void ip_lane_real(v2& x, v2 P, v2 S) {
+    asm("{\n\t.reg .b32 a, b;\n\t.reg .b64 s, t;\n\t"
+        "mov.b64 {a, b}, %0;\n\tmov.b64 s, {b, a};\n\t"
+        "mul.rn.f32x2 t, %1, %0;\n\tfma.rn.f32x2 %0, %2, s, t;\n\t}"
+        : "+l"(x) : "l"(P), "l"(S));
+}
+// x <- K x + swap(x)  (H: K = (1, -1))
+__device__ __forceinline__ void ip_lane_h(v2& x, v2 K) {
+    asm("{\n\t.reg .b32 a, b;\n\t.reg .b64 s;\n\t"
+        "mov.b64 {a, b}, %0;\n\tmov.b64 s, {b, a};\n\tfma.rn.f32x2 %0, %1, %0, s;\n\t}"
+        : "+l"(x) : "l"(K));
+}
+// x <- x + K swap(x)  (sqrt(Y): K = (-1, 1))
+__device__ __forceinline__ void ip_lane_y(v2& x, v2 K) {
+    asm("{\n\t.reg .b32 a, b;\n\t.reg .b64 s;\n\t"
+        "mov.b64 {a, b}, %0;\n\tmov.b64 s, {b, a};\n\tfma.rn.f32x2 %0, %1, s, %0;\n\t}"
+        : "+l"(x) : "l"(K));
+}
+// sqrt(X) without its 1/sqrt2 on the lane: re <- re + swap(im), im <- im - swap(re)
+__device__ __forceinline__ void ip_lane_sx(v2& r, v2& i) {
+    asm("{\n\t.reg .b32 a, b, c, d;\n\t.reg .b64 s, u;\n\t"
+        "mov.b64 {a, b}, %0;\n\tmov.b64 s, {b, a};\n\t"
+        "mov.b64 {c, d}, %1;\n\tmov.b64 u, {d, c};\n\t"
+        "add.rn.f32x2 %0, %0, u;\n\tsub.rn.f32x2 %1, %1, s;\n\t}"
+        : "+l"(r), "+l"(i));
+}
+// [[a, i b], [i c, d]] on the lane: re <- P re + Xn swap(im), im <- P im + X swap(re)
+// with P = (a, d), X = (b, c), Xn = -X
+__device__ __forceinline__ void ip_lane_imoff(v2& r, v2& i, v2 P, v2 X, v2 Xn) {
+    asm("{\n\t.reg .b32 a, b, c, d;\n\t.reg .b64 s, u, t;\n\t"
+        "mov.b64 {a, b}, %0;\n\tmov.b64 s, {b, a};\n\t"
+        "mov.b64 {c, d}, %1;\n\tmov.b64 u, {d, c};\n\t"
+        "mul.rn.f32x2 t, %2, %0;\n\tfma.rn.f32x2 %0, %4, u, t;\n\t"
+        "mul.rn.f32x2 t, %2, %1;\n\tfma.rn.f32x2 %1, %3, s, t;\n\t}"
+        : "+l"(r), "+l"(i) : "l"(P), "l"(X), "l"(Xn));
+}
+
+template <int NV>
+__device__ __forceinline__ void lane_real(Amps<NV>& A, const float (&m)[8], uint32_t creg) {
+    const v2 P = vpack(m[0], m[6]), S = vpack(m[2], m[4]);
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+        if ((uint32_t(2 * j) & creg) != creg) continue;
+        ip_lane_real(A.re[j], P, S);
+        ip_lane_real(A.im[j], P, S);
+    }
+}
+
+template <int NV>
+__device__ __forceinline__ void lane_imoff(Amps<NV>& A, const float (&m)[8], uint32_t creg) {
+    const v2 P = vpack(m[0], m[6]), X = vpack(m[3], m[5]), Xn = vpack(-m[3], -m[5]);
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+        if ((uint32_t(2 * j) & creg) != creg) continue;
+        ip_lane_imoff(A.re[j], A.im[j], P, X, Xn);
+    }
+}
+
+// H, sqrt(Y), sqrt(X) without their 1/sqrt2 (deferred to the phase scale):
+// H: (lo + hi, lo - hi); sqrt(Y): (lo - hi, lo + hi); sqrt(X): (lo - i hi, hi - i lo)
+template <int KIND, int NV>
+__device__ __forceinline__ void lane_had(Amps<NV>& A, uint32_t creg) {
+    const v2 K = KIND == OP_H ? vpack(1.f, -1.f) : vpack(-1.f, 1.f);
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+        if ((uint32_t(2 * j) & creg) != creg) continue;
+        if (KIND == OP_H) {
+            ip_lane_h(A.re[j], K);
+            ip_lane_h(A.im[j], K);
+        } else if (KIND == OP_SY) {
+            ip_lane_y(A.re[j], K);
+            ip_lane_y(A.im[j], K);
+        } else {
+            ip_lane_sx(A.re[j], A.im[j]);
+        }
+    }
+}
+
 // ---- register-controlled ops on bit J >= 1: compute, then keep per lane ----------
 __device__ __forceinline__ v2 pick(bool o0, bool o1, v2 nw, v2 old) {
     if (o0 && o1) return nw;
@@ -431,8 +514,11 @@ __device__ __forceinline__ void apply_op(Amps<(1 << (R - 1))>& A, const uint4 hd
         HQ_CASE_LANE(OP_DREG, (lane_diag<NV>(A, m, creg)))
         HQ_CASE_LANE(OP_NEGHI, (lane_diag<NV>(A, m, creg)))
         HQ_CASE_LANE(OP_U, (lane_u<NV>(A, m, creg)))
-        HQ_CASE_LANE(OP_REAL, (lane_u<NV>(A, m, creg)))
-        HQ_CASE_LANE(OP_IMOFF, (lane_u<NV>(A, m, creg)))
+        HQ_CASE_LANE(OP_REAL, (lane_real<NV>(A, m, creg)))
+        HQ_CASE_LANE(OP_IMOFF, (lane_imoff<NV>(A, m, creg)))
+        HQ_CASE_LANE(OP_H, (lane_had<OP_H, NV>(A, creg)))
+        HQ_CASE_LANE(OP_SY, (lane_had<OP_SY, NV>(A, creg)))
+        HQ_CASE_LANE(OP_SX, (lane_had<OP_SX, NV>(A, creg)))
         HQ_CASE_J(0, OP_U, (op_u<J, NV>(A, m)))
         HQ_CASE_J(0, OP_REAL, (op_real<J, NV>(A, m)))
         HQ_CASE_J(0, OP_IMOFF, (op_imoff<J, NV>(A, m)))
