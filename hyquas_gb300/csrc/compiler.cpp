@@ -576,14 +576,17 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
     int pending_count = 0;
     std::vector<char> done(gates.size(), 0);
     size_t ndone = 0;
-    while (ndone < gates.size()) {
-        // register qubits of this phase: local qubit 0 always (the f32x2 lane),
-        // plus up to r-1 targets chosen greedily in gate order
-        uint32_t rset = 1u;
+    // The gates of the next phase given the gates done so far, and its register
+    // qubits: local qubit 0 always (the f32x2 lane), plus up to r-1 targets
+    // chosen greedily in gate order, padded with the tile qubits fewest of the
+    // phase's diagonal gates target (a diagonal gate off the register set is a
+    // per-thread scalar instead of a multiply per amplitude).
+    auto choose = [&](const std::vector<char>& dn, std::vector<int>& members, uint32_t& rset) {
+        rset = 1u;
+        members.clear();
         uint64_t blocked = 0;
-        std::vector<int> members;
         for (size_t i = 0; i < gates.size(); i++) {
-            if (done[i]) continue;
+            if (dn[i]) continue;
             const hq_gate& g = gates[i];
             const uint64_t q = gate_qubits(g);
             if (q & blocked) {
@@ -602,23 +605,77 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
             }
             members.push_back((int)i);
         }
+        std::vector<int> score(k, 0);
+        for (int i : members)
+            if (diag[i] && loc[gates[i].target] >= 0) score[loc[gates[i].target]]++;
+        // ties go to the highest tile qubits: the low ones stay thread bits, where
+        // they give whole 32-byte sectors to the stores of neighbouring threads
+        std::vector<int> cand;
+        for (int b = k - 1; b >= 1; b--)
+            if (!((rset >> b) & 1)) cand.push_back(b);
+        std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) { return score[a] < score[b]; });
+        for (int b : cand) {
+            if (__builtin_popcount(rset) >= r) break;
+            rset |= 1u << b;
+        }
+    };
+    // a diagonal gate that the kernels run as a per-thread complex factor when
+    // its target is a thread bit (not a pure sign, no register control)
+    auto thread_factor = [&](int i, uint32_t rset) {
+        const hq_gate& g = gates[i];
+        if (!diag[i]) return false;
+        const int lt = loc[g.target];
+        if (lt >= 0 && ((rset >> lt) & 1)) return false;
+        for (int c : {g.control, g.control2})
+            if (c >= 0 && loc[c] >= 0 && ((rset >> loc[c]) & 1)) return false;
+        const bool sign = g.mat[0] == 1.0 && g.mat[1] == 0.0 && g.mat[6] == -1.0 && g.mat[7] == 0.0;
+        return !sign;
+    };
+    while (ndone < gates.size()) {
+        std::vector<int> members;
+        uint32_t rset;
+        choose(done, members, rset);
         HQ_REQUIRE(!members.empty(), HQ_ERR_INVALID, "oshm: planner made no progress");
-        // pad the register set with the tile qubits fewest of this phase's
-        // diagonal gates target (a diagonal gate off the register set is a
-        // per-thread scalar instead of a multiply per amplitude)
+        // A single-qubit diagonal gate on a register qubit (other than the lane)
+        // that no later non-diagonal gate of the phase targets can wait for the
+        // next phase (it commutes with everything between).  Where its qubit is
+        // a thread bit there, it is a per-thread factor instead of arithmetic on
+        // every amplitude (about 16 packed operations per thread), but a phase
+        // with such factors pays a complex multiply of its amplitudes (about 32
+        // more): the gates wait when the next phase, planned ahead, gains.
         {
-            std::vector<int> score(k, 0);
-            for (int i : members)
-                if (diag[i] && loc[gates[i].target] >= 0) score[loc[gates[i].target]]++;
-            // ties go to the highest tile qubits: the low ones stay thread bits, where
-            // they give whole 32-byte sectors to the stores of neighbouring threads
-            std::vector<int> cand;
-            for (int b = k - 1; b >= 1; b--)
-                if (!((rset >> b) & 1)) cand.push_back(b);
-            std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) { return score[a] < score[b]; });
-            for (int b : cand) {
-                if (__builtin_popcount(rset) >= r) break;
-                rset |= 1u << b;
+            std::vector<int> keep, later;
+            for (size_t a = 0; a < members.size(); a++) {
+                const int i = members[a];
+                const hq_gate& g = gates[i];
+                const int lt = loc[g.target];
+                bool wait = diag[i] && g.control < 0 && g.control2 < 0 && lt > 0 && ((rset >> lt) & 1);
+                for (size_t b = a + 1; wait && b < members.size(); b++)
+                    if (!diag[members[b]] && gates[members[b]].target == g.target) wait = false;
+                (wait ? later : keep).push_back(i);
+            }
+            if (!later.empty() && !keep.empty() && ndone + members.size() < gates.size()) {
+                std::vector<char> dn = done;
+                for (int i : keep) dn[i] = 1;
+                std::vector<int> next;
+                uint32_t nrset;
+                choose(dn, next, nrset);
+                std::vector<char> is_later(gates.size(), 0);
+                for (int i : later) is_later[i] = 1;
+                bool acc = false;
+                for (int i : next)
+                    if (!is_later[i] && thread_factor(i, nrset)) acc = true;
+                std::vector<int> moved;
+                for (int i : later)
+                    if (thread_factor(i, nrset)) moved.push_back(i);
+                if (moved.size() * 16 > (acc ? 0u : 32u)) {
+                    std::vector<char> is_moved(gates.size(), 0);
+                    for (int i : moved) is_moved[i] = 1;
+                    std::vector<int> m2;
+                    for (int i : members)
+                        if (!is_moved[i]) m2.push_back(i);
+                    members.swap(m2);
+                }
             }
         }
 

@@ -178,46 +178,81 @@ struct Gen {
               << (k1 ? "true" : "false") << ");\n";
     }
 
-    // Per-slot signed scales within a phase: register vector j (and its
-    // imaginary partner) holds sigma_j = (neg_j ? -1 : 1) sqrt(2)^e_j times its
-    // true amplitudes.  Exact 45-degree phases (T, T^dagger) then cost one add
-    // per component, the slot's scale growing by sqrt 2; a sign flip on a
-    // register qubit (Z, CZ) only flips the slot's sign; the adds of H, sqrt(X)
-    // and sqrt(Y) absorb a scale ratio as one FMA; the phase's closing multiply
-    // divides every slot by its scale.
+    // Per-lane signed scales within a phase: lane l of register vector j (and
+    // of its imaginary partner), flat index 2 j + l, holds
+    // sigma = (neg ? -1 : 1) sqrt(2)^e times its true amplitude.  Exact
+    // 45-degree phases (T, T^dagger) then cost one add per component, the
+    // scale growing by sqrt 2; a sign flip on a register qubit (Z, CZ) only
+    // flips the sign; the adds of H, sqrt(X) and sqrt(Y) absorb a scale ratio
+    // as one FMA (a packed constant when the two lanes' ratios differ); the
+    // phase's closing multiply divides every lane by its scale.
     std::vector<int> se;
     std::vector<char> sn;
     void reset_scales() {
-        se.assign(nv, 0);
-        sn.assign(nv, 0);
+        se.assign(2 * nv, 0);
+        sn.assign(2 * nv, 0);
     }
-    double sigma(int j) const {
-        double r = std::ldexp(1.0, se[j] >= 0 ? se[j] / 2 : -((-se[j]) / 2));
-        if (se[j] & 1) r = se[j] > 0 ? r * std::sqrt(2.0) : r / std::sqrt(2.0);
-        return (sn[j] ? -1.0 : 1.0) * r;
+    double sigma(int x) const {
+        double r = std::ldexp(1.0, se[x] >= 0 ? se[x] / 2 : -((-se[x]) / 2));
+        if (se[x] & 1) r = se[x] > 0 ? r * std::sqrt(2.0) : r / std::sqrt(2.0);
+        return (sn[x] ? -1.0 : 1.0) * r;
     }
-    // sigma_a / sigma_b, exact for even exponent differences
+    // sigma_a / sigma_b (flat indices), exact for even exponent differences
     double ratio(int a, int b) const {
         const int d = se[a] - se[b];
         double r = std::ldexp(1.0, d >= 0 ? d / 2 : -((-d) / 2));
         if (d & 1) r = d > 0 ? r * std::sqrt(2.0) : r / std::sqrt(2.0);
         return (sn[a] != sn[b] ? -1.0 : 1.0) * r;
     }
+    // lane l of slot a over lane l of slot b
+    double ra(int a, int b, int l) const { return ratio(2 * a + l, 2 * b + l); }
     static std::string vconst(double x) { return "vdup(" + flit((float)x) + ")"; }
-    // base + k * other as one instruction
-    static std::string comb(const std::string& base, double k, const std::string& other) {
-        if (k == 1.0) return "vadd(" + base + ", " + other + ")";
-        if (k == -1.0) return "vsub(" + base + ", " + other + ")";
-        return "vfma(" + vconst(k) + ", " + other + ", " + base + ")";
+    // k0 in the low lane, k1 in the high one
+    static std::string kpair(double k0, double k1) {
+        if ((float)k0 == (float)k1) return vconst(k0);
+        return "vpack(" + flit((float)k0) + ", " + flit((float)k1) + ")";
     }
-    // give slot h the scale of slot j (two multiplies)
-    void align(int j, int h) {
-        if (se[h] == se[j] && sn[h] == sn[j]) return;
-        const std::string k = vconst(ratio(j, h));
-        o << R(h) << " = vmul(" << k << ", " << R(h) << "); " << I(h) << " = vmul(" << k << ", " << I(h)
+    // base + k * other as one instruction, k per lane
+    static std::string comb(const std::string& base, double k0, double k1, const std::string& other) {
+        if (k0 == 1.0 && k1 == 1.0) return "vadd(" + base + ", " + other + ")";
+        if (k0 == -1.0 && k1 == -1.0) return "vsub(" + base + ", " + other + ")";
+        return "vfma(" + kpair(k0, k1) + ", " + other + ", " + base + ")";
+    }
+    static std::string comb(const std::string& base, double k, const std::string& other) {
+        return comb(base, k, k, other);
+    }
+    bool same(int a, int b) const { return se[a] == se[b] && sn[a] == sn[b]; }
+    // v *= k for the lanes' factors k0, k1: sign flips only as bit XORs (ALU
+    // pipe), anything else as one multiply per component
+    void rescale(int j, double k0, double k1) {
+        if (k0 == 1.0 && k1 == 1.0) return;
+        if (std::fabs(k0) == 1.0 && std::fabs(k1) == 1.0) {
+            const char* mask = k0 < 0 && k1 < 0 ? "0x8000000080000000ull"
+                                                 : (k0 < 0 ? "0x80000000ull" : "0x8000000000000000ull");
+            o << R(j) << " ^= " << mask << "; " << I(j) << " ^= " << mask << ";\n";
+            return;
+        }
+        const std::string k = kpair(k0, k1);
+        o << R(j) << " = vmul(" << k << ", " << R(j) << "); " << I(j) << " = vmul(" << k << ", " << I(j)
           << ");\n";
-        se[h] = se[j];
-        sn[h] = sn[j];
+    }
+    // give slot h the scales of slot j
+    void align(int j, int h) {
+        rescale(h, ra(j, h, 0), ra(j, h, 1));
+        for (int l = 0; l < 2; l++) {
+            se[2 * h + l] = se[2 * j + l];
+            sn[2 * h + l] = sn[2 * j + l];
+        }
+    }
+    // give lane 1 of slot j the scale of its lane 0
+    void align_lanes(int j) {
+        rescale(j, 1.0, ratio(2 * j, 2 * j + 1));
+        se[2 * j + 1] = se[2 * j];
+        sn[2 * j + 1] = sn[2 * j];
+    }
+    void flip(int j) {
+        sn[2 * j] = !sn[2 * j];
+        sn[2 * j + 1] = !sn[2 * j + 1];
     }
 
     // scaled forms: sqrt(X) / sqrt(Y) keep both scales, so they also run under a
@@ -248,6 +283,10 @@ struct Gen {
                 if ((k0 || k1) && pair_needs_align(kind, k0 && k1, has_cout)) align(j, j | (1 << (J - 1)));
             }
         }
+        // an exchange of the lanes under a run-time control needs them at one scale
+        if (kind == OP_X && J == 0 && has_cout)
+            for (int j = 0; j < nv; j++)
+                if ((uint32_t(2 * j) & op.creg) == op.creg) align_lanes(j);
         if (has_cout) o << "if ((pidx & " << hex64(op.cout) << ") == " << hex64(op.cout) << ") {\n";
         o << "{\n";
         if (kind == OP_DOUT) {
@@ -297,15 +336,39 @@ struct Gen {
         }
         if (J == 0) {
             // target = the vector lane
+            const double h2 = std::sqrt(0.5);
+            const bool lane_rot45 = kind == OP_DREG && !has_cout && m[0] == 1.f && m[1] == 0.f &&
+                                    std::fabs(std::fabs(m[6]) - h2) < 1e-6 && std::fabs(std::fabs(m[7]) - h2) < 1e-6;
             if (kind == OP_X) {
                 for (int j = 0; j < nv; j++) {
                     if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
                     o << R(j) << " = vswap(" << R(j) << "); " << I(j) << " = vswap(" << I(j) << ");\n";
+                    if (!has_cout) {  // the lanes' scales go with their values
+                        std::swap(se[2 * j], se[2 * j + 1]);
+                        std::swap(sn[2 * j], sn[2 * j + 1]);
+                    }
                 }
             } else if (kind == OP_NEGHI) {
                 for (int j = 0; j < nv; j++) {
                     if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
-                    o << R(j) << " ^= 0x8000000000000000ull; " << I(j) << " ^= 0x8000000000000000ull;\n";
+                    if (!has_cout)  // a sign: folded into the high lane's scale
+                        sn[2 * j + 1] = !sn[2 * j + 1];
+                    else
+                        o << R(j) << " ^= 0x8000000000000000ull; " << I(j) << " ^= 0x8000000000000000ull;\n";
+                }
+            } else if (lane_rot45) {
+                // T or T^dagger on the lane: the high lane's (x, y) -> (x + t y, y - t x), its
+                // scale growing by sqrt 2 (negated when the real part of the phase is -1)
+                const double c = m[6] > 0 ? 1.0 : -1.0, sgn = m[7] > 0 ? 1.0 : -1.0;
+                const double t = c > 0 ? -sgn : sgn;
+                o << "const v2 Kt = vpack(0.f, " << flit((float)t) << "), Ktn = vpack(0.f, " << flit((float)-t)
+                  << ");\n";
+                for (int j = 0; j < nv; j++) {
+                    if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
+                    o << "{ const v2 a = " << R(j) << ", b = " << I(j) << "; " << R(j) << " = vfma(Kt, b, a); "
+                      << I(j) << " = vfma(Ktn, a, b); }\n";
+                    se[2 * j + 1] += 1;
+                    if (c < 0) sn[2 * j + 1] = !sn[2 * j + 1];
                 }
             } else if (kind == OP_DREG) {
                 const float d0r = m[0], d0i = m[1], d1r = m[6], d1i = m[7];
@@ -317,56 +380,52 @@ struct Gen {
                     o << "{ const v2 a = " << R(j) << ", b = " << I(j) << "; " << R(j)
                       << " = vfma(In, b, vmul(Rr, a)); " << I(j) << " = vfma(Ii, a, vmul(Rr, b)); }\n";
                 }
-            } else if (kind == OP_REAL || kind == OP_IMOFF || kind == OP_H || kind == OP_SY ||
-                       kind == OP_SX) {
-                // the other lane from a swapped copy, both lanes' coefficients in
-                // one packed constant: one or two instructions per component (the
-                // two lanes of a vector always share their scale)
-                if (kind == OP_REAL)
-                    o << "const v2 P = vpack(" << flit(m[0]) << ", " << flit(m[6]) << "), S = vpack("
-                      << flit(m[2]) << ", " << flit(m[4]) << ");\n";
-                else if (kind == OP_IMOFF)
-                    o << "const v2 P = vpack(" << flit(m[0]) << ", " << flit(m[6]) << "), X = vpack("
-                      << flit(m[3]) << ", " << flit(m[5]) << "), Xn = vpack(" << flit(-m[3]) << ", "
-                      << flit(-m[5]) << ");\n";
-                else if (kind == OP_H)
-                    o << "const v2 K = vpack(1.f, -1.f);\n";
-                else if (kind == OP_SY)
-                    o << "const v2 K = vpack(-1.f, 1.f);\n";
+            } else {
+                // the other lane from a swapped copy, both lanes' coefficients in one
+                // packed constant that also absorbs the ratio of the lanes' scales:
+                // one or two instructions per component for the structured
+                // matrices, four for a general one
+                const bool gen = kind == OP_U || kind == OP_DREG || kind == OP_DROT || kind == OP_RROT;
+                if (kind == OP_REAL || kind == OP_IMOFF || gen)
+                    o << "const v2 P = vpack(" << flit(m[0]) << ", " << flit(m[6]) << ");\n";
+                if (gen)
+                    o << "const v2 Q = vpack(" << flit(m[1]) << ", " << flit(m[7]) << "), Qn = vpack("
+                      << flit(-m[1]) << ", " << flit(-m[7]) << ");\n";
                 for (int j = 0; j < nv; j++) {
                     if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
+                    const double r01 = ratio(2 * j, 2 * j + 1), r10 = ratio(2 * j + 1, 2 * j);
                     o << "{ const v2 a = " << R(j) << ", b = " << I(j) << ", as = vswap(a), bs = vswap(b); ";
-                    switch (kind) {
-                        case OP_REAL:  // (a lo + b hi, c lo + d hi)
-                            o << R(j) << " = vfma(S, as, vmul(P, a)); " << I(j) << " = vfma(S, bs, vmul(P, b));";
-                            break;
-                        case OP_IMOFF:  // (a lo + i b hi, i c lo + d hi)
-                            o << R(j) << " = vfma(Xn, bs, vmul(P, a)); " << I(j) << " = vfma(X, as, vmul(P, b));";
-                            break;
-                        case OP_H:  // (lo + hi, lo - hi)
-                            o << R(j) << " = vfma(K, a, as); " << I(j) << " = vfma(K, b, bs);";
-                            break;
-                        case OP_SY:  // (lo - hi, lo + hi)
-                            o << R(j) << " = vfma(K, as, a); " << I(j) << " = vfma(K, bs, b);";
-                            break;
-                        default:  // sqrt(X): (lo - i hi, hi - i lo)
+                    if (kind == OP_REAL) {  // (a lo + b hi, c lo + d hi)
+                        const std::string S = kpair(m[2] * r01, m[4] * r10);
+                        o << R(j) << " = vfma(" << S << ", as, vmul(P, a)); " << I(j) << " = vfma(" << S
+                          << ", bs, vmul(P, b));";
+                    } else if (kind == OP_IMOFF) {  // (a lo + i b hi, i c lo + d hi)
+                        o << R(j) << " = vfma(" << kpair(-m[3] * r01, -m[5] * r10) << ", bs, vmul(P, a)); "
+                          << I(j) << " = vfma(" << kpair(m[3] * r01, m[5] * r10) << ", as, vmul(P, b));";
+                    } else if (kind == OP_H && !has_cout) {  // (lo + hi, hi - lo): the high lane negated
+                        const std::string K = kpair(r01, -r10);
+                        o << R(j) << " = vfma(" << K << ", as, a); " << I(j) << " = vfma(" << K << ", bs, b);";
+                        sn[2 * j + 1] = !sn[2 * j + 1];
+                    } else if (kind == OP_H) {  // (lo + hi, lo - hi)
+                        const std::string K = kpair(r01, r10), pm = kpair(1.0, -1.0);
+                        o << R(j) << " = vfma(" << pm << ", a, vmul(" << K << ", as)); " << I(j) << " = vfma("
+                          << pm << ", b, vmul(" << K << ", bs));";
+                    } else if (kind == OP_SY) {  // (lo - hi, lo + hi)
+                        const std::string K = kpair(-r01, r10);
+                        o << R(j) << " = vfma(" << K << ", as, a); " << I(j) << " = vfma(" << K << ", bs, b);";
+                    } else if (kind == OP_SX) {  // (lo - i hi, hi - i lo)
+                        if (r01 == 1.0 && r10 == 1.0)
                             o << R(j) << " = vadd(a, bs); " << I(j) << " = vsub(b, as);";
-                            break;
+                        else
+                            o << R(j) << " = vfma(" << kpair(r01, r10) << ", bs, a); " << I(j) << " = vfma("
+                              << kpair(-r01, -r10) << ", as, b);";
+                    } else {  // general complex 2x2
+                        const std::string S = kpair(m[2] * r01, m[4] * r10), T = kpair(m[3] * r01, m[5] * r10),
+                                          Tn = kpair(-m[3] * r01, -m[5] * r10);
+                        o << R(j) << " = vfma(" << Tn << ", bs, vfma(" << S << ", as, vfma(Qn, b, vmul(P, a)))); "
+                          << I(j) << " = vfma(" << T << ", as, vfma(" << S << ", bs, vfma(Q, a, vmul(P, b))));";
                     }
                     o << " }\n";
-                }
-            } else {
-                o << "const v2 P = vpack(" << flit(m[0]) << ", " << flit(m[6]) << "), Q = vpack("
-                  << flit(m[1]) << ", " << flit(m[7]) << "), Qn = vpack(" << flit(-m[1]) << ", "
-                  << flit(-m[7]) << "), S = vpack(" << flit(m[2]) << ", " << flit(m[4])
-                  << "), T = vpack(" << flit(m[3]) << ", " << flit(m[5]) << "), Tn = vpack("
-                  << flit(-m[3]) << ", " << flit(-m[5]) << ");\n";
-                for (int j = 0; j < nv; j++) {
-                    if ((uint32_t(2 * j) & op.creg) != op.creg) continue;
-                    o << "{ const v2 a = " << R(j) << ", b = " << I(j)
-                      << ", as = vswap(a), bs = vswap(b); " << R(j)
-                      << " = vfma(Tn, bs, vfma(S, as, vfma(Qn, b, vmul(P, a)))); " << I(j)
-                      << " = vfma(T, as, vfma(S, bs, vfma(Q, a, vmul(P, b)))); }\n";
                 }
             }
             o << "}\n";
@@ -434,35 +493,38 @@ struct Gen {
             if (!k0 && !k1) continue;
             const bool full = k0 && k1;
             const bool fast = pair_fast(kind, full, has_cout);
-            if (kind == OP_NEGHI && full && !has_cout) {  // a sign: folded into the slot's scale
-                sn[h] = !sn[h];
+            if (kind == OP_NEGHI && !has_cout) {  // a sign: folded into the lanes' scales
+                if (k0) sn[2 * h] = !sn[2 * h];
+                if (k1) sn[2 * h + 1] = !sn[2 * h + 1];
                 continue;
             }
             o << "{ const v2 lr = " << R(j) << ", li = " << I(j) << ", hr = " << R(h) << ", hi = " << I(h)
               << ";\n";
             if (fast && (kind == OP_H || kind == OP_SY || kind == OP_SX)) {
-                const double rj = ratio(j, h), rh = ratio(h, j);
+                const double rj0 = ra(j, h, 0), rj1 = ra(j, h, 1), rh0 = ra(h, j, 0), rh1 = ra(h, j, 1);
                 if (kind == OP_H) {  // L' = L + H, H' = L - H (stored as H - L, scale negated)
-                    o << R(j) << " = " << comb("lr", rj, "hr") << "; " << I(j) << " = " << comb("li", rj, "hi")
-                      << "; " << R(h) << " = " << comb("hr", -rh, "lr") << "; " << I(h) << " = "
-                      << comb("hi", -rh, "li") << ";\n";
-                    sn[h] = !sn[h];
+                    o << R(j) << " = " << comb("lr", rj0, rj1, "hr") << "; " << I(j) << " = "
+                      << comb("li", rj0, rj1, "hi") << "; " << R(h) << " = " << comb("hr", -rh0, -rh1, "lr") << "; "
+                      << I(h) << " = " << comb("hi", -rh0, -rh1, "li") << ";\n";
+                    flip(h);
                 } else if (kind == OP_SY) {  // L' = L - H, H' = L + H
-                    o << R(j) << " = " << comb("lr", -rj, "hr") << "; " << I(j) << " = "
-                      << comb("li", -rj, "hi") << "; " << R(h) << " = " << comb("hr", rh, "lr") << "; " << I(h)
-                      << " = " << comb("hi", rh, "li") << ";\n";
+                    o << R(j) << " = " << comb("lr", -rj0, -rj1, "hr") << "; " << I(j) << " = "
+                      << comb("li", -rj0, -rj1, "hi") << "; " << R(h) << " = " << comb("hr", rh0, rh1, "lr") << "; "
+                      << I(h) << " = " << comb("hi", rh0, rh1, "li") << ";\n";
                 } else {  // L' = L - i H, H' = H - i L
-                    o << R(j) << " = " << comb("lr", rj, "hi") << "; " << I(j) << " = "
-                      << comb("li", -rj, "hr") << "; " << R(h) << " = " << comb("hr", rh, "li") << "; " << I(h)
-                      << " = " << comb("hi", -rh, "lr") << ";\n";
+                    o << R(j) << " = " << comb("lr", rj0, rj1, "hi") << "; " << I(j) << " = "
+                      << comb("li", -rj0, -rj1, "hr") << "; " << R(h) << " = " << comb("hr", rh0, rh1, "li") << "; "
+                      << I(h) << " = " << comb("hi", -rh0, -rh1, "lr") << ";\n";
                 }
                 o << "}\n";
                 continue;
             }
             if (fast && kind == OP_X) {
                 o << R(j) << " = hr; " << I(j) << " = hi; " << R(h) << " = lr; " << I(h) << " = li;\n}\n";
-                std::swap(se[j], se[h]);
-                std::swap(sn[j], sn[h]);
+                for (int l = 0; l < 2; l++) {
+                    std::swap(se[2 * j + l], se[2 * h + l]);
+                    std::swap(sn[2 * j + l], sn[2 * h + l]);
+                }
                 continue;
             }
             if (full && rot45) {
@@ -474,8 +536,9 @@ struct Gen {
                 else
                     o << R(h) << " = " << comb("hr", sgn, "hi") << "; " << I(h) << " = " << comb("hi", -sgn, "hr")
                       << ";\n}\n";
-                se[h] += 1;
-                if (c < 0) sn[h] = !sn[h];
+                se[2 * h] += 1;
+                se[2 * h + 1] += 1;
+                if (c < 0) flip(h);
                 continue;
             }
             switch (kind) {
@@ -544,8 +607,8 @@ struct Gen {
                         o << (comp ? I(j) : R(j)) << " = x; " << (comp ? I(h) : R(h)) << " = y; }\n";
                     }
                     if (negf_op && !has_cout) {
-                        sn[j] = !sn[j];
-                        sn[h] = !sn[h];
+                        flip(j);
+                        flip(h);
                     }
                     break;
                 }
@@ -766,15 +829,58 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
         bool uses_acc = false;
         g.uses_neg = false;
         g.reset_scales();
-        for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) g.op(prog.ops[oi], uses_acc);
-        // closing multiply: the phase's deferred scale and the per-thread factor,
-        // each slot divided by its own scale
-        std::vector<double> kf(NV);
-        bool any_k = false;
-        for (int j = 0; j < NV; j++) {
-            kf[j] = double(P.scale) / g.sigma(j);
-            any_k = any_k || (float)kf[j] != 1.f;
+        // A phase whose closing multiply would be the per-thread factor alone
+        // (every lane's scale 1 at its end) applies that factor first: the ops
+        // that make it (diagonals on thread bits, no register control) commute
+        // with the phase's other ops.  The same arithmetic, but NVRTC has
+        // scheduled the factor-only block at the phase end far worse (a
+        // 30-qubit group: 5.2 against 3.1 ms).
+        auto is_factor = [](const OshmOp& op) { return op.kind == OP_DOUT && op.creg == 0; };
+        bool early = false;
+        bool has_factor = false;
+        for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) has_factor = has_factor || is_factor(prog.ops[oi]);
+        if (has_factor) {
+            Gen d;
+            d.nv = g.nv;
+            d.reset_scales();
+            bool ua = false;
+            for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) d.op(prog.ops[oi], ua);
+            bool ones = true;
+            for (int x = 0; x < 2 * NV; x++) ones = ones && (float)(double(P.scale) / d.sigma(x)) == 1.f;
+            early = ua && ones;
         }
+        if (early) {
+            for (uint32_t oi = P.op_begin; oi < P.op_end; oi++)
+                if (is_factor(prog.ops[oi])) g.op(prog.ops[oi], uses_acc);
+            if (g.uses_neg) o << "if (negf) { acc.x = -acc.x; acc.y = -acc.y; }\n";
+            o << "{ const float2 f = acc;\nconst v2 fr = vdup(f.x), fi = vdup(f.y), fin = vdup(-f.y);\n";
+            for (int j = 0; j < NV; j++)
+                o << "{ const v2 a = r" << j << ", b = i" << j << "; r" << j << " = vfma(fin, b, vmul(fr, a)); i"
+                  << j << " = vfma(fi, a, vmul(fr, b)); }\n";
+            o << "}\n";
+            for (uint32_t oi = P.op_begin; oi < P.op_end; oi++)
+                if (!is_factor(prog.ops[oi])) g.op(prog.ops[oi], uses_acc);
+            uses_acc = false;  // applied; every lane's scale ends at 1
+            g.uses_neg = false;
+        } else {
+            for (uint32_t oi = P.op_begin; oi < P.op_end; oi++) g.op(prog.ops[oi], uses_acc);
+        }
+        // closing multiply: the phase's deferred scale and the per-thread factor,
+        // each lane divided by its own scale
+        std::vector<float> kf(2 * NV);
+        bool any_k = false;
+        for (int x = 0; x < 2 * NV; x++) {
+            kf[x] = (float)(double(P.scale) / g.sigma(x));
+            any_k = any_k || kf[x] != 1.f;
+        }
+        // the packed factor of vector j, each lane's constant times `mul` (a run-time
+        // float expression) or plain
+        auto kvec = [&](int j, const std::string& mul) {
+            const float k0 = kf[2 * j], k1 = kf[2 * j + 1];
+            const std::string s0 = mul.empty() ? flit(k0) : mul + " * " + flit(k0);
+            if (k0 == k1) return "vdup(" + s0 + ")";
+            return "vpack(" + s0 + ", " + (mul.empty() ? flit(k1) : mul + " * " + flit(k1)) + ")";
+        };
         const bool neg_in_mul = g.uses_neg && !uses_acc && any_k;  // the sign rides on the multiply
         if (g.uses_neg && uses_acc) {
             o << "if (negf) { acc.x = -acc.x; acc.y = -acc.y; }\n";
@@ -786,35 +892,35 @@ std::string generate(const OshmProgram& prog, int& threads, size_t& smem, Shape 
             o << "}\n";
         }
         if (uses_acc) {
+            // the vectors sharing a factor together, each factor in a scope of its
+            // own: few factors are live at once (with many, NVRTC's schedule of
+            // the block has measured 1.6x slower)
             o << "{ const float2 f = acc;\n";
-            std::map<float, int> names;
+            std::map<std::pair<float, float>, std::vector<int>> by_factor;
+            std::vector<std::pair<float, float>> order;
             for (int j = 0; j < NV; j++) {
-                const float k = (float)kf[j];
-                auto it = names.find(k);
-                if (it == names.end()) {
-                    const int q = (int)names.size();
-                    names[k] = q;
-                    o << "const v2 fr" << q << " = vdup(f.x * " << flit(k) << "), fi" << q << " = vdup(f.y * "
-                      << flit(k) << "), fin" << q << " = vdup(-f.y * " << flit(k) << ");\n";
-                }
-                const int q = names[k];
-                o << "{ const v2 a = r" << j << ", b = i" << j << "; r" << j << " = vfma(fin" << q
-                  << ", b, vmul(fr" << q << ", a)); i" << j << " = vfma(fi" << q << ", a, vmul(fr" << q
-                  << ", b)); }\n";
+                const std::pair<float, float> key(kf[2 * j], kf[2 * j + 1]);
+                if (!by_factor.count(key)) order.push_back(key);
+                by_factor[key].push_back(j);
+            }
+            for (const auto& key : order) {
+                const std::vector<int>& js = by_factor[key];
+                o << "{ const v2 fr = " << kvec(js[0], "f.x") << ", fi = " << kvec(js[0], "f.y")
+                  << ", fin = " << kvec(js[0], "-f.y") << ";\n";
+                for (int j : js)
+                    o << "{ const v2 a = r" << j << ", b = i" << j << "; r" << j
+                      << " = vfma(fin, b, vmul(fr, a)); i" << j << " = vfma(fi, a, vmul(fr, b)); }\n";
+                o << "}\n";
             }
             o << "}\n";
         } else if (neg_in_mul) {
             o << "{ const float ns = negf ? -1.f : 1.f;\n";
             for (int j = 0; j < NV; j++)
-                o << "{ const v2 k = vdup(" << flit((float)kf[j]) << " * ns); r" << j << " = vmul(k, r" << j
-                  << "); i" << j << " = vmul(k, i" << j << "); }\n";
+                o << "{ const v2 k = " << kvec(j, "ns") << "; r" << j << " = vmul(k, r" << j << "); i" << j
+                  << " = vmul(k, i" << j << "); }\n";
             o << "}\n";
         } else if (any_k) {
-            for (int j = 0; j < NV; j++) {
-                if ((float)kf[j] == 1.f) continue;
-                o << "r" << j << " = vmul(" << Gen::vconst(kf[j]) << ", r" << j << "); i" << j << " = vmul("
-                  << Gen::vconst(kf[j]) << ", i" << j << ");\n";
-            }
+            for (int j = 0; j < NV; j++) g.rescale(j, kf[2 * j], kf[2 * j + 1]);
         }
         if (lastp) {
             // vector j holds the amplitudes at pidx | (its register bits) and + 1
@@ -939,6 +1045,41 @@ Shape first_shape() {
     return Shape::RING;
 }
 
+// Generated sources by program (its bytes; phases and ops are zero-filled
+// before they are set, so equal programs have equal bytes) and shape: a
+// circuit compiled again skips the generator.
+struct GenEntry {
+    std::string src;
+    int threads = 0;
+    size_t smem = 0;
+};
+std::mutex g_gen_mu;
+std::map<std::string, GenEntry> g_gen;
+
+std::string generate_cached(const OshmProgram& p, int& threads, size_t& smem, Shape shape) {
+    std::string key;
+    const int32_t hdr[4] = {p.n, p.k, p.r, (int32_t)shape};
+    key.append((const char*)hdr, sizeof(hdr));
+    key.append((const char*)&p.tile_mask, sizeof(p.tile_mask));
+    key.append((const char*)p.phases.data(), p.phases.size() * sizeof(OshmPhase));
+    key.append((const char*)p.ops.data(), p.ops.size() * sizeof(OshmOp));
+    {
+        std::lock_guard<std::mutex> lk(g_gen_mu);
+        auto it = g_gen.find(key);
+        if (it != g_gen.end()) {
+            threads = it->second.threads;
+            smem = it->second.smem;
+            return it->second.src;
+        }
+    }
+    GenEntry e;
+    e.src = generate(p, e.threads, e.smem, shape);
+    threads = e.threads;
+    smem = e.smem;
+    std::lock_guard<std::mutex> lk(g_gen_mu);
+    return g_gen.emplace(std::move(key), std::move(e)).first->second.src;
+}
+
 std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>& progs) {
     ensure_init();
     const Shape shape0 = first_shape();
@@ -946,7 +1087,7 @@ std::vector<JitKernel> jit_compile_groups(const std::vector<const OshmProgram*>&
     std::vector<int> threads(progs.size());
     std::vector<size_t> smem(progs.size());
     for (size_t i = 0; i < progs.size(); i++)
-        srcs[i] = generate(*progs[i], threads[i], smem[i], shape0);
+        srcs[i] = generate_cached(*progs[i], threads[i], smem[i], shape0);
     std::vector<std::shared_ptr<CacheEntry>> ents(progs.size());
     std::vector<size_t> todo;
     {
@@ -1040,7 +1181,7 @@ bool jit_lookup_cached(const std::vector<const OshmProgram*>& progs, std::vector
     for (const OshmProgram* pr : progs) {
         int t = 0;
         size_t sm = 0;
-        const std::string src = generate(*pr, t, sm, shape0);
+        const std::string src = generate_cached(*pr, t, sm, shape0);
         std::shared_ptr<CacheEntry> e;
         {
             std::lock_guard<std::mutex> lk(g_cache_mu);

@@ -456,6 +456,56 @@ def test_generated_kernels_clifford_t(hq, oracle, n, seed):
     check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
 
 
+def lane_heavy_circuit(seed, n, count):
+    """Half of the gates on physical qubit 0 (the packed vectors' lane): the
+    closed forms and scale bookkeeping of gates there (T and T^dagger as one
+    add on the high lane, H / sqrt(X) / sqrt(Y), real and imaginary
+    off-diagonal 2x2s and general ones absorbing the lanes' scale ratio, sign
+    flips folded into a lane's scale, lane exchanges under register and
+    run-time controls), mixed with the same gates on the other qubits."""
+    rng = W.SplitMix64(seed)
+    half = math.pi / 2
+    out = []
+    for _ in range(count):
+        qs = list(rng.shuffle(range(n))[:3])
+        if rng.below(2) == 0:
+            j = rng.below(2)
+            if 0 in qs:
+                qs.remove(0)
+            qs.insert(j, 0)
+        k = rng.below(16)
+        th = rng.uniform() * W.TWO_PI
+        one = [(W.H, ()), (W.RX, (half,)), (W.RY, (half,)), (W.T, ()), (W.TDG, ()), (W.S, ()),
+               (W.X, ()), (W.Z, ()), (W.Y, ()), (W.RY, (th,)), (W.RX, (th,)),
+               (W.U3, (th, 0.3, 1.1))]
+        if k < len(one):
+            t, p = one[k]
+            out.append((t, qs[0], -1, -1, p))
+        elif k == 12:
+            out.append((W.CZ, qs[1], qs[0], -1, ()))
+        elif k == 13:
+            out.append((W.CNOT, qs[1], qs[0], -1, ()))
+        elif k == 14:
+            out.append((W.CNOT, qs[0], qs[1], -1, ()))
+        else:
+            out.append((W.CU1, qs[0], qs[1], -1, (math.pi / 4,)))
+    return out
+
+
+@pytest.mark.parametrize("specialize", [0, 1])
+@pytest.mark.parametrize("n,seed,tile", [(9, 1, 8), (14, 2, 10), (17, 3, 13)])
+def test_lane_heavy_circuits(hq, oracle, n, seed, tile, specialize):
+    desc = lane_heavy_circuit(800 + seed, n, 700)
+    c = hq.Circuit(n)
+    c.addGates(W.to_gates(desc))
+    c.compile("oshm", tile_qubits=tile, specialize=specialize)
+    psi = W.random_state(50 + seed, n)
+    s = hq.State(n, zero=False)
+    s.load(psi)
+    c.run_on(s)
+    check(oracle, oracle.apply_f64(n, psi.astype(np.complex128), desc), s.store())
+
+
 @pytest.mark.parametrize("rows,cols", [(4, 4), (3, 6)])
 def test_grid_circuit_small_vs_oracle(hq, oracle, rows, cols):
     n = rows * cols
