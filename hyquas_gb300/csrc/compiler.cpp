@@ -678,6 +678,25 @@ OshmProgram plan_oshm(int n, const std::vector<hq_gate>& gates, uint64_t tile_ma
                 }
             }
         }
+        // The phase's per-thread factors wait for the next phase when all of them
+        // can: their qubits are thread bits there too (so they stay per-thread
+        // factors), and this phase saves the complex multiply that applies them.
+        {
+            std::vector<int> fac, rest;
+            for (int i : members) (thread_factor(i, rset) ? fac : rest).push_back(i);
+            if (!fac.empty() && !rest.empty() && ndone + members.size() < gates.size()) {
+                std::vector<char> dn = done;
+                for (int i : rest) dn[i] = 1;
+                std::vector<int> next;
+                uint32_t nrset;
+                choose(dn, next, nrset);
+                std::vector<char> in_next(gates.size(), 0);
+                for (int i : next) in_next[i] = 1;
+                bool all = true;
+                for (int i : fac) all = all && in_next[i] && thread_factor(i, nrset);
+                if (all) members.swap(rest);
+            }
+        }
 
         OshmPhase ph;
         std::memset(&ph, 0, sizeof(ph));
